@@ -1,0 +1,213 @@
+"""ctypes front-end of the CPU oracle (test infrastructure only).
+
+Loads ``oracle/_build/libqporacle.so`` (built from ``qp_oracle.cpp`` by
+``oracle/Makefile``).  Only the tests, the smoke check and the CPU-baseline
+leg of the bench use it, as the checker; the product path never does.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import subprocess
+
+import numpy as np
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+_LIB_PATH = os.path.join(_HERE, "_build", "libqporacle.so")
+_lib = None
+
+_dp = np.ctypeslib.ndpointer(dtype=np.float64, flags="C_CONTIGUOUS")
+_u64p = np.ctypeslib.ndpointer(dtype=np.uint64, flags="C_CONTIGUOUS")
+_i32p = np.ctypeslib.ndpointer(dtype=np.int32, flags="C_CONTIGUOUS")
+_i8p = np.ctypeslib.ndpointer(dtype=np.int8, flags="C_CONTIGUOUS")
+
+
+def build(force: bool = False) -> str:
+    if force or not os.path.exists(_LIB_PATH) or \
+            os.path.getmtime(_LIB_PATH) < os.path.getmtime(os.path.join(_HERE, "qp_oracle.cpp")):
+        subprocess.run(["make", "-s", "-C", _HERE], check=True)
+    return _LIB_PATH
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        build()
+        L = C.CDLL(_LIB_PATH)
+        L.qpo_create.argtypes = [C.c_int, C.c_int, C.c_int, _dp, _dp, C.POINTER(C.c_void_p)]
+        L.qpo_destroy.argtypes = [C.c_void_p]
+        L.qpo_set_dets.argtypes = [C.c_void_p, _u64p, C.c_int64]
+        L.qpo_ref_energy.argtypes = [C.c_void_p]
+        L.qpo_ref_energy.restype = C.c_double
+        L.qpo_n_unique.argtypes = [C.c_void_p, C.POINTER(C.c_int), C.POINTER(C.c_int)]
+        L.qpo_tables.argtypes = [C.c_void_p] + [C.c_void_p] * 5
+        L.qpo_bilinear.argtypes = [C.c_void_p] + [_i32p] * 8
+        L.qpo_unique_strings.argtypes = [C.c_void_p, _u64p, _u64p]
+        L.qpo_h_s2_u0_work.argtypes = [C.c_void_p, _dp, _dp, _dp, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int]
+        L.qpo_h_s2_u0.argtypes = [C.c_void_p, _dp, _dp, _dp, C.c_int, C.c_int64]
+        L.qpo_connected_pairs.argtypes = [C.c_void_p, _i32p, _i32p, _i8p, C.c_int64]
+        L.qpo_connected_pairs.restype = C.c_int64
+        L.qpo_pair_excitation.argtypes = [C.c_void_p, C.c_int32, C.c_int32, C.c_int, _i32p,
+                                          C.POINTER(C.c_double), C.POINTER(C.c_double)]
+        L.qpo_diag.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p]
+        L.qpo_i_h_j.argtypes = [C.c_void_p, _u64p, _u64p]
+        L.qpo_i_h_j.restype = C.c_double
+        L.qpo_get_s2.argtypes = [C.c_void_p, _u64p, _u64p]
+        L.qpo_get_s2.restype = C.c_double
+        L.qpo_dense.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p]
+        L.qpo_davidson.argtypes = [C.c_void_p, _dp, C.c_int64, _dp, _dp, C.c_int, C.c_int, C.c_int,
+                                   C.c_double, C.c_int, C.c_int, _dp]
+        L.qpo_num_threads.restype = C.c_int
+        _lib = L
+    return _lib
+
+
+def _ptr(a):
+    return a.ctypes.data_as(C.c_void_p) if a is not None else None
+
+
+class Oracle:
+    """FP64 restatement of the reference's sigma / Slater rules / Davidson."""
+
+    def __init__(self, n_mo, n_alpha, n_beta, h, eri, dets=None):
+        L = lib()
+        self.n_mo, self.n_alpha, self.n_beta = n_mo, n_alpha, n_beta
+        self.n_int = (n_mo - 1) // 64 + 1
+        hf = np.ascontiguousarray(np.asarray(h, dtype=np.float64).T)  # col-major
+        self._h = C.c_void_p()
+        rc = L.qpo_create(n_mo, n_alpha, n_beta, hf.ravel(), np.ascontiguousarray(eri, dtype=np.float64),
+                          C.byref(self._h))
+        if rc != 0:
+            raise ValueError(f"qpo_create failed ({rc})")
+        self.n_det = 0
+        if dets is not None:
+            self.set_dets(dets)
+
+    @classmethod
+    def from_problem(cls, prob):
+        return cls(prob.n_mo, prob.n_alpha, prob.n_beta, prob.ints.h, prob.ints.eri, prob.dets)
+
+    def __del__(self):
+        if getattr(self, "_h", None) is not None and _lib is not None:
+            _lib.qpo_destroy(self._h)
+            self._h = None
+
+    def set_dets(self, dets):
+        dets = np.ascontiguousarray(dets, dtype=np.uint64)
+        self.dets = dets
+        self.n_det = dets.shape[0]
+        rc = lib().qpo_set_dets(self._h, dets.ravel(), self.n_det)
+        if rc != 0:
+            raise ValueError(f"qpo_set_dets failed ({rc})")
+
+    @property
+    def ref_energy(self):
+        return lib().qpo_ref_energy(self._h)
+
+    def n_unique(self):
+        a, b = C.c_int(), C.c_int()
+        lib().qpo_n_unique(self._h, C.byref(a), C.byref(b))
+        return a.value, b.value
+
+    def tables(self):
+        n = self.n_mo
+        f, jj, kk = (np.empty((n, n)) for _ in range(3))
+        bc, bx = np.empty((n, n, n)), np.empty((n, n, n))
+        lib().qpo_tables(self._h, _ptr(f), _ptr(jj), _ptr(kk), _ptr(bc), _ptr(bx))
+        # col-major -> index [i-1, j-1] with transpose
+        return dict(fock=f.T.copy(), jj=jj.T.copy(), kk=kk.T.copy(),
+                    big_coul=bc.transpose(2, 1, 0).copy(), big_exch=bx.transpose(2, 1, 0).copy())
+
+    def bilinear(self):
+        N = self.n_det
+        ua, ub = self.n_unique()
+        arrs = [np.empty(N, np.int32) for _ in range(6)]
+        cl = np.empty(ub + 1, np.int32)
+        rl = np.empty(ua + 1, np.int32)
+        lib().qpo_bilinear(self._h, *arrs, cl, rl)
+        keys = ["rows", "cols", "order", "t_rows", "t_cols", "t_order"]
+        d = dict(zip(keys, arrs))
+        d["col_loc"], d["row_loc"] = cl, rl
+        a = np.empty((ua, self.n_int), np.uint64)
+        b = np.empty((ub, self.n_int), np.uint64)
+        lib().qpo_unique_strings(self._h, a.ravel(), b.ravel())
+        d["alpha_unique"], d["beta_unique"] = a, b
+        return d
+
+    def h_s2_u0(self, u0):
+        """u0: (N_st, N) -> (v0, s0) each (N_st, N)  [H_S2_u_0_nstates_openmp]."""
+        u0 = np.ascontiguousarray(np.atleast_2d(u0), dtype=np.float64)
+        nst, n = u0.shape
+        v = np.zeros_like(u0)
+        s = np.zeros_like(u0)
+        rc = lib().qpo_h_s2_u0(self._h, v.ravel(), s.ravel(), u0.ravel(), nst, n)
+        if rc != 0:
+            raise ValueError(f"qpo_h_s2_u0 failed ({rc})")
+        return v, s
+
+    def h_s2_u0_work(self, u_t, istart, iend, ishift=0, istep=1):
+        """Range variant in bilinear order; u_t: (N, N_st) states fastest."""
+        u_t = np.ascontiguousarray(u_t, dtype=np.float64)
+        nst = u_t.shape[1]
+        v = np.zeros_like(u_t)
+        s = np.zeros_like(u_t)
+        rc = lib().qpo_h_s2_u0_work(self._h, v.ravel(), s.ravel(), u_t.ravel(), nst, istart, iend, ishift, istep)
+        if rc != 0:
+            raise ValueError(f"qpo_h_s2_u0_work failed ({rc})")
+        return v, s
+
+    def connected_pairs(self):
+        """(I, J, cls) arrays (0-based original order), sorted by (I, J)."""
+        L = lib()
+        empty32 = np.empty(1, np.int32)
+        n = L.qpo_connected_pairs(self._h, empty32, empty32, np.empty(1, np.int8), 0)
+        I = np.empty(n, np.int32)
+        J = np.empty(n, np.int32)
+        cls = np.empty(n, np.int8)
+        L.qpo_connected_pairs(self._h, I, J, cls, n)
+        o = np.lexsort((J, I))
+        return I[o], J[o], cls[o]
+
+    def pair_excitation(self, i, j, cls):
+        exc = np.zeros(4, np.int32)
+        hij, sij = C.c_double(), C.c_double()
+        ph = lib().qpo_pair_excitation(self._h, int(i), int(j), int(cls), exc, C.byref(hij), C.byref(sij))
+        return ph, exc, hij.value, sij.value
+
+    def diag(self):
+        h = np.empty(self.n_det)
+        s = np.empty(self.n_det)
+        lib().qpo_diag(self._h, _ptr(h), _ptr(s))
+        return h, s
+
+    def i_h_j(self, di, dj):
+        return lib().qpo_i_h_j(self._h, np.ascontiguousarray(di, np.uint64).ravel(),
+                               np.ascontiguousarray(dj, np.uint64).ravel())
+
+    def get_s2(self, di, dj):
+        return lib().qpo_get_s2(self._h, np.ascontiguousarray(di, np.uint64).ravel(),
+                                np.ascontiguousarray(dj, np.uint64).ravel())
+
+    def dense(self, with_s2=True):
+        N = self.n_det
+        H = np.empty((N, N))
+        S = np.empty((N, N)) if with_s2 else None
+        lib().qpo_dense(self._h, _ptr(H), _ptr(S))
+        return H, S
+
+    def davidson(self, guess, n_states, davidson_sze_max=8, threshold=1e-12, s2_eig=True, max_sigma=0):
+        """guess: (N_st_diag, N).  Returns (energies, s2, vectors, n_sigma, residuals)."""
+        u = np.ascontiguousarray(guess, dtype=np.float64).copy()
+        nsd, n = u.shape
+        e = np.zeros(nsd)
+        s2 = np.zeros(nsd)
+        res = np.zeros(max(n_states, 1))
+        rc = lib().qpo_davidson(self._h, u.ravel(), n, e, s2, n_states, nsd, davidson_sze_max,
+                                threshold, int(bool(s2_eig)), max_sigma, res)
+        if rc < 0:
+            raise RuntimeError(f"qpo_davidson failed ({rc})")
+        return e, s2, u, rc, res
+
+
+def num_threads() -> int:
+    return lib().qpo_num_threads()
