@@ -1,0 +1,130 @@
+/*
+ * qpgpu.h -- C ABI of the GB300 (sm_103a) Davidson sigma library.
+ *
+ * Drop-in boundary for Quantum Package's sigma path.  Each entry point names
+ * the reference routine (path:line in the quantum_package source tree) whose
+ * role it takes; the Fortran host binds them through iso_c_binding.
+ *
+ * Conventions
+ *  - Every call returns an int status: QPGPU_OK (0) or a negative QPGPU_ERR_*;
+ *    qpgpu_last_error() gives the message of the last failure of a context.
+ *    The reference stops the program instead (diagonalization_hs2.irp.f:110-114,
+ *    404-409); the Fortran shim turns a non-zero status into `stop`.
+ *  - Orbitals are 1-based; determinants are psi_det(N_int,2,N) int64 bit
+ *    strings (Fortran order: for det k, alpha words then beta words).
+ *  - Vectors u_0(sze,N_st) are column-major double precision, leading
+ *    dimension `ld` >= N_det, determinants in psi_det order.
+ *  - "host" arguments are host pointers (the call copies); "device" arguments
+ *    are device pointers on the context's GPU.
+ *  - A context may be used by one host thread at a time (calls lock it).
+ */
+#ifndef QPGPU_H
+#define QPGPU_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define QPGPU_OK 0
+#define QPGPU_ERR_ARG (-1)      /* invalid argument (shape, null pointer, range) */
+#define QPGPU_ERR_STATE (-2)    /* integrals / determinants not set */
+#define QPGPU_ERR_CUDA (-3)     /* CUDA runtime error */
+#define QPGPU_ERR_NOMEM (-4)    /* device allocation failed */
+#define QPGPU_ERR_DAVIDSON (-5) /* Davidson failed (residual > 1e8) */
+#define QPGPU_ERR_TIMEOUT (-6)  /* a bounded device wait ran out */
+#define QPGPU_ERR_NUMERIC (-7)  /* NaN / Inf in an input vector */
+
+/* Arithmetic of a sigma application. */
+#define QPGPU_FP64 0  /* FP64 matrix elements and products */
+#define QPGPU_FP32 1  /* FP32 elements and products, Kahan-compensated per-row sums,
+                         FP64 diagonal */
+
+typedef struct qpgpu_ctx qpgpu_ctx;
+
+typedef struct qpgpu_info {
+  int64_t n_det;          /* N_det */
+  int32_t n_alpha_unique; /* N_det_alpha_unique */
+  int32_t n_beta_unique;  /* N_det_beta_unique */
+  int64_t n_pairs;        /* directed connected pairs (I != J, degree 1-2) */
+  int64_t n_s2_pairs;     /* pairs with <I|S^2|J> != 0 */
+  double setup_ms;        /* device time of the last qpgpu_set_dets */
+  double ref_energy;      /* ref_bitmask_energy */
+  int64_t device_bytes;   /* device memory held by the context */
+} qpgpu_info;
+
+/* Context for one orbital space; replaces the IRPF90 providers N_int,
+ * elec_alpha_num, elec_beta_num, mo_tot_num (src/Bitmask/bitmasks.irp.f:3-15).
+ * n_int must be (n_mo-1)/64+1 and at most 2 (n_mo <= 128).  n_alpha >= n_beta
+ * as in src/Bitmask/bitmasks.irp.f:82. */
+int qpgpu_create(int n_mo, int n_alpha, int n_beta, int n_int, qpgpu_ctx** out);
+int qpgpu_destroy(qpgpu_ctx* ctx);
+const char* qpgpu_last_error(qpgpu_ctx* ctx);
+int qpgpu_get_info(qpgpu_ctx* ctx, qpgpu_info* info);
+
+/* Integrals (host).  h_pq: n_mo x n_mo column-major, symmetric
+ * (mo_mono_elec_integral, src/Integrals_Monoelec/mo_mono_ints.irp.f:1-26).
+ * eri_packed: chemist (pq|rs) at bielec_integrals_index key - 1
+ * (src/Integrals_Bielec/map_integrals.irp.f:19-34), P2*(P2+1)/2 entries with
+ * P2 = n_mo*(n_mo+1)/2.  Derives on the device mo_bielec_integral_jj /
+ * _jj_anti (mo_bi_integrals.irp.f:1344-1369), big_array_coulomb/exchange
+ * (integrals_3_index.irp.f:1-22), the closed-shell Fock operator
+ * (mono_excitations.irp.f:22-95) and ref_bitmask_energy (ref_bitmask.irp.f:1-56).
+ * Replaces the integral hash map / dense cache.  Invalidates determinant data. */
+int qpgpu_set_integrals(qpgpu_ctx* ctx, const double* h_pq, const double* eri_packed);
+
+/* Determinants (host, psi_det(N_int,2,n_det)).  Builds on the device the
+ * bilinear alpha x beta index (spindeterminants.irp.f:56-596), the connected
+ * pairs with their FP64/FP32 matrix elements, H_II and <I|S^2|I>.  This is the
+ * provider rebuild the reference performs after TOUCH psi_det. */
+int qpgpu_set_dets(qpgpu_ctx* ctx, const uint64_t* psi_det, int64_t n_det);
+
+/* H_S2_u_0_nstates_openmp (src/Davidson/u0Hu0.irp.f:15-66), host arrays:
+ * v_0 = H u_0 and s_0 = S^2 u_0 (S^2 without the S_z(S_z-1) shift, as the
+ * reference), each (ld, n_st) column-major.  u_0 is read only. */
+int qpgpu_h_s2_u0(qpgpu_ctx* ctx, double* v0, double* s0, const double* u0, int n_st, int64_t ld);
+
+/* H_S2_u_0_nstates_openmp_work (src/Davidson/u0Hu0.irp.f:69-96), host arrays
+ * in bilinear order, states fastest: u_t(n_st, N_det), v_t, s_t.  Only rows
+ * k = istart+ishift, istart+ishift+istep, ..., <= iend (1-based) are written;
+ * other rows of v_t, s_t are left untouched. */
+int qpgpu_h_s2_u0_work(qpgpu_ctx* ctx, double* v_t, double* s_t, const double* u_t, int n_st, int istart,
+                       int iend, int ishift, int istep);
+
+/* Device variant of qpgpu_h_s2_u0: same layout, device pointers, runs on the
+ * given CUDA stream (NULL: the context's stream), precision QPGPU_FP64 or
+ * QPGPU_FP32.  Asynchronous. */
+int qpgpu_h_s2_u0_device(qpgpu_ctx* ctx, double* v0, double* s0, const double* u0, int n_st, int64_t ld,
+                         int precision, void* stream);
+
+/* Sigma in the internal layout: u_t, v_t, s_t are device arrays (N_det, n_st)
+ * with states fastest, determinants in bilinear order (the order of
+ * qpgpu_bilinear_order).  u_t32 (FP32 copy of u_t) is required for
+ * QPGPU_FP32 and ignored otherwise.  Asynchronous on `stream`. */
+int qpgpu_sigma_bilinear(qpgpu_ctx* ctx, double* v_t, double* s_t, const double* u_t, const float* u_t32,
+                         int n_st, int precision, void* stream);
+
+/* psi_bilinear_matrix_order (spindeterminants.irp.f:387-445), 0-based, host:
+ * order[k] = psi_det index of bilinear position k. */
+int qpgpu_bilinear_order(qpgpu_ctx* ctx, int32_t* order);
+
+/* H_jj(i) = diag_H_mat_elem(psi_det(:,:,i)) (davidson_diag_hs2,
+ * src/Davidson/diagonalization_hs2.irp.f:37-45) and diag_S_mat_elem, host,
+ * psi_det order.  Either pointer may be NULL. */
+int qpgpu_diag(qpgpu_ctx* ctx, double* h_jj, double* s_jj);
+
+/* Debug export of the connected pairs sigma visits, host, psi_det indices
+ * (0-based): class 1 alpha single, 2 beta single, 3 alpha double, 4 beta
+ * double, 5 alpha-beta double; phase +1/-1; exc = (h1,p1,h2,p2) 1-based
+ * (get_mono/double_excitation_spin, slater_rules.irp.f:2783-2987; for class 5
+ * alpha (h,p) then beta (h,p)); hij = FP64 <I|H|J>.  *n_pairs returns the
+ * total; at most `cap` records are written (pass cap = 0 to query). */
+int qpgpu_connected_pairs(qpgpu_ctx* ctx, int64_t* n_pairs, int32_t* I, int32_t* J, int8_t* cls,
+                          int8_t* phase, int16_t* exc, double* hij, int64_t cap);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* QPGPU_H */

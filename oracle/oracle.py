@@ -49,6 +49,7 @@ def lib():
         L.qpo_connected_pairs.restype = C.c_int64
         L.qpo_pair_excitation.argtypes = [C.c_void_p, C.c_int32, C.c_int32, C.c_int, _i32p,
                                           C.POINTER(C.c_double), C.POINTER(C.c_double)]
+        L.qpo_pair_excitations.argtypes = [C.c_void_p, C.c_int64, _i32p, _i32p, _i8p, _i8p, _i32p, _dp, _dp]
         L.qpo_diag.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p]
         L.qpo_i_h_j.argtypes = [C.c_void_p, _u64p, _u64p]
         L.qpo_i_h_j.restype = C.c_double
@@ -173,6 +174,19 @@ class Oracle:
         hij, sij = C.c_double(), C.c_double()
         ph = lib().qpo_pair_excitation(self._h, int(i), int(j), int(cls), exc, C.byref(hij), C.byref(sij))
         return ph, exc, hij.value, sij.value
+
+    def pair_excitations(self, I, J, cls):
+        """Batched pair_excitation: (phase int8, exc (n,4) int32, hij, sij)."""
+        n = len(I)
+        ph = np.empty(n, np.int8)
+        exc = np.empty((n, 4), np.int32)
+        hij = np.empty(n)
+        sij = np.empty(n)
+        rc = lib().qpo_pair_excitations(self._h, n, np.ascontiguousarray(I, np.int32), np.ascontiguousarray(J, np.int32),
+                                        np.ascontiguousarray(cls, np.int8), ph, exc.ravel(), hij, sij)
+        if rc != 0:
+            raise RuntimeError("qpo_pair_excitations failed")
+        return ph, exc, hij, sij
 
     def diag(self):
         h = np.empty(self.n_det)

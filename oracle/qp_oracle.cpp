@@ -1281,3 +1281,17 @@ int qpo_num_threads(void) {
 }
 
 }  // extern "C"
+
+extern "C" {
+// Batched qpo_pair_excitation over n pairs (OpenMP): phase (+1/-1), exc[4*i..], hij, sij.
+int qpo_pair_excitations(qpo_ctx* hc, int64_t n, const int32_t* I, const int32_t* J, const int8_t* cls,
+                         int8_t* phase, int32_t* exc, double* hij, double* sij) {
+  int bad = 0;
+#pragma omp parallel for schedule(static) reduction(| : bad)
+  for (int64_t i = 0; i < n; ++i) {
+    int ph = qpo_pair_excitation(hc, I[i], J[i], cls[i], exc + 4 * i, hij + i, sij + i);
+    if (ph == -1 || ph == 1) phase[i] = (int8_t)ph; else bad = 1;
+  }
+  return bad ? -1 : 0;
+}
+}

@@ -1,0 +1,500 @@
+// Build of the connected-pair Hamiltonian (CSR over bilinear rows).
+//
+// The pair set is the one H_S2_u_0_nstates_openmp_work visits
+// (src/Davidson/u0Hu0.irp.f:177-444): for the determinant I = (a, b) at
+// bilinear position k
+//   class A  J in the same beta column, alpha strings 1 or 2 apart  (:277-332)
+//   class B  J in the same alpha row, beta strings 1 or 2 apart      (:336-415)
+//   class C  alpha single x beta single                              (:177-246)
+// with the diagonal kept apart (:418-441).  Row k's segment of the CSR holds
+// its A hits (column order), then B hits (row order), then C hits.
+//
+// Two passes run the same deterministic traversal: the first counts hits per
+// row, the second writes them (column = bilinear position of J, FP64 and FP32
+// matrix elements).  Same-spin classes scan a column (row) with one thread per
+// determinant; the column's strings are staged in shared memory and read by
+// every thread of the block as broadcasts.  Class C gives one warp per row and
+// compacts hits with __ballot_sync, scanning either the columns of the beta
+// singles of b (as the reference does) or the rows of the alpha singles of a,
+// whichever holds fewer determinants.
+#include <cub/cub.cuh>
+
+#include "qpgpu_internal.cuh"
+
+namespace {
+
+constexpr int BLK = 256;
+constexpr int TILE = 1024;
+
+inline unsigned nblocks(int64_t n, int tpb) {
+  int64_t g = (n + tpb - 1) / tpb;
+  return (unsigned)(g < 1 ? 1 : g);
+}
+
+template <class T>
+struct Scoped {
+  T* p = nullptr;
+  ~Scoped() { dev_free(p); }
+};
+
+struct BuildArgs {
+  DevTables t;
+  int64_t N;
+  const u64* alpha;
+  const u64* beta;
+  const int* rows;
+  const int* cols;
+  const int* col_loc;
+  const int* t_order;
+  const int* t_cols;
+  const int* row_loc;
+  const int* sa_ptr;
+  const int* sa_idx;
+  const int* sb_ptr;
+  const int* sb_idx;
+  const int64_t* cost_a;
+  const int64_t* cost_b;
+  // counts (count pass output, fill pass input)
+  int* cntA;
+  int* cntB;
+  int* cntC;
+  int* cntS;
+  // CSR (fill pass)
+  const int64_t* rowptr;
+  int* colidx;
+  double* val64;
+  float* val32;
+  const int64_t* s2ptr;
+  int* s2col;
+  float* s2val;
+  int* err;  // set when a fill pass would write past its row's segment
+};
+
+// ---- class A: same beta column, alpha singles / doubles -------------------
+template <int NINT, bool FILL>
+__global__ void __launch_bounds__(BLK) k_class_a(BuildArgs a) {
+  __shared__ u64 tile[TILE * NINT];
+  const int64_t r0 = (int64_t)blockIdx.x * BLK;
+  if (r0 >= a.N) return;
+  const int64_t k = r0 + threadIdx.x;
+  const bool valid = k < a.N;
+  const int64_t rl = min(r0 + BLK, a.N) - 1;
+  const int U0 = a.col_loc[a.cols[r0]];
+  const int U1 = a.col_loc[a.cols[rl] + 1];
+  int cs = 0, ce = 0;
+  u64 my[2 * NINT];
+  int64_t out = 0;
+  if (valid) {
+    const int b = a.cols[k];
+    cs = a.col_loc[b];
+    ce = a.col_loc[b + 1];
+    const int ai = a.rows[k];
+#pragma unroll
+    for (int w = 0; w < NINT; ++w) {
+      my[w] = a.alpha[(int64_t)ai * NINT + w];
+      my[NINT + w] = a.beta[(int64_t)b * NINT + w];
+    }
+    if (FILL) out = a.rowptr[k];
+  }
+  int cnt = 0;
+  for (int t0 = U0; t0 < U1; t0 += TILE) {
+    const int tn = min(TILE, U1 - t0);
+    __syncthreads();
+    for (int i = threadIdx.x; i < tn; i += BLK) {
+      const int ai = a.rows[t0 + i];
+#pragma unroll
+      for (int w = 0; w < NINT; ++w) tile[i * NINT + w] = a.alpha[(int64_t)ai * NINT + w];
+    }
+    __syncthreads();
+    if (valid) {
+      const int lo = max(cs, t0), hi = min(ce, t0 + tn);
+      for (int pos = lo; pos < hi; ++pos) {
+        const u64* c = &tile[(pos - t0) * NINT];
+        int d = 0;
+#pragma unroll
+        for (int w = 0; w < NINT; ++w) d += popc64(my[w] ^ c[w]);
+        if (d == 2 || d == 4) {
+          if (FILL) {
+            u64 J[2 * NINT];
+#pragma unroll
+            for (int w = 0; w < NINT; ++w) {
+              J[w] = c[w];
+              J[NINT + w] = my[NINT + w];
+            }
+            double v = (d == 2) ? h_mono_spin<NINT>(a.t, my, J, 1, nullptr, nullptr)
+                                : h_double_spin<NINT>(a.t, my, c, nullptr, nullptr);
+            if (cnt < a.cntA[k]) {
+              a.colidx[out + cnt] = pos;
+              a.val64[out + cnt] = v;
+              a.val32[out + cnt] = (float)v;
+            } else {
+              atomicOr(a.err, 1);
+            }
+          }
+          ++cnt;
+        }
+      }
+    }
+  }
+  if (!FILL && valid) a.cntA[k] = cnt;
+}
+
+// ---- class B: same alpha row, beta singles / doubles ----------------------
+template <int NINT, bool FILL>
+__global__ void __launch_bounds__(BLK) k_class_b(BuildArgs a) {
+  __shared__ u64 tile[TILE * NINT];
+  const int64_t q0 = (int64_t)blockIdx.x * BLK;
+  if (q0 >= a.N) return;
+  const int64_t q = q0 + threadIdx.x;
+  const bool valid = q < a.N;
+  const int64_t ql = min(q0 + BLK, a.N) - 1;
+  const int V0 = a.row_loc[a.rows[a.t_order[q0]]];
+  const int V1 = a.row_loc[a.rows[a.t_order[ql]] + 1];
+  int rs = 0, re = 0;
+  int64_t k = 0, out = 0;
+  u64 my[2 * NINT];
+  if (valid) {
+    k = a.t_order[q];
+    const int ai = a.rows[k], bi = a.cols[k];
+    rs = a.row_loc[ai];
+    re = a.row_loc[ai + 1];
+#pragma unroll
+    for (int w = 0; w < NINT; ++w) {
+      my[w] = a.alpha[(int64_t)ai * NINT + w];
+      my[NINT + w] = a.beta[(int64_t)bi * NINT + w];
+    }
+    if (FILL) out = a.rowptr[k] + a.cntA[k];
+  }
+  int cnt = 0;
+  for (int t0 = V0; t0 < V1; t0 += TILE) {
+    const int tn = min(TILE, V1 - t0);
+    __syncthreads();
+    for (int i = threadIdx.x; i < tn; i += BLK) {
+      const int bi = a.t_cols[t0 + i];
+#pragma unroll
+      for (int w = 0; w < NINT; ++w) tile[i * NINT + w] = a.beta[(int64_t)bi * NINT + w];
+    }
+    __syncthreads();
+    if (valid) {
+      const int lo = max(rs, t0), hi = min(re, t0 + tn);
+      for (int pos = lo; pos < hi; ++pos) {
+        const u64* c = &tile[(pos - t0) * NINT];
+        int d = 0;
+#pragma unroll
+        for (int w = 0; w < NINT; ++w) d += popc64(my[NINT + w] ^ c[w]);
+        if (d == 2 || d == 4) {
+          if (FILL) {
+            u64 J[2 * NINT];
+#pragma unroll
+            for (int w = 0; w < NINT; ++w) {
+              J[w] = my[w];
+              J[NINT + w] = c[w];
+            }
+            double v = (d == 2) ? h_mono_spin<NINT>(a.t, my, J, 2, nullptr, nullptr)
+                                : h_double_spin<NINT>(a.t, my + NINT, c, nullptr, nullptr);
+            if (cnt < a.cntB[k]) {
+              a.colidx[out + cnt] = a.t_order[pos];
+              a.val64[out + cnt] = v;
+              a.val32[out + cnt] = (float)v;
+            } else {
+              atomicOr(a.err, 2);
+            }
+          }
+          ++cnt;
+        }
+      }
+    }
+  }
+  if (!FILL && valid) a.cntB[k] = cnt;
+}
+
+// spin flip test of an alpha-single x beta-single pair: the two excitations
+// swap the same two orbitals between the spins (get_s2, s2.irp.f:46-55)
+template <int NINT>
+__device__ __forceinline__ bool spin_flip(const u64* my, const u64* ca, const u64* cb) {
+  bool same = true, core = false;
+#pragma unroll
+  for (int w = 0; w < NINT; ++w) {
+    u64 xa = my[w] ^ ca[w], xb = my[NINT + w] ^ cb[w];
+    same &= (xa == xb);
+    core |= (xa & my[w] & my[NINT + w]) != 0;
+  }
+  return same && !core;
+}
+
+// ---- class C: alpha single x beta single, one warp per row ----------------
+template <int NINT, bool FILL>
+__global__ void __launch_bounds__(BLK) k_class_c(BuildArgs a) {
+  const int lane = threadIdx.x & 31;
+  const int64_t warp = ((int64_t)blockIdx.x * BLK + threadIdx.x) >> 5;
+  const int64_t nwarp = ((int64_t)gridDim.x * BLK) >> 5;
+  const unsigned lt = (1u << lane) - 1u;
+  for (int64_t k = warp; k < a.N; k += nwarp) {
+    const int ai = a.rows[k], bi = a.cols[k];
+    u64 my[2 * NINT];
+#pragma unroll
+    for (int w = 0; w < NINT; ++w) {
+      my[w] = a.alpha[(int64_t)ai * NINT + w];
+      my[NINT + w] = a.beta[(int64_t)bi * NINT + w];
+    }
+    int64_t out = 0, sout = 0;
+    if (FILL) {
+      out = a.rowptr[k] + a.cntA[k] + a.cntB[k];
+      sout = a.s2ptr[k];
+    }
+    int cnt = 0, scnt = 0;
+    const bool by_cols = a.cost_b[bi] <= a.cost_a[ai];
+    if (by_cols) {
+      for (int t = a.sb_ptr[bi]; t < a.sb_ptr[bi + 1]; ++t) {
+        const int bp = a.sb_idx[t];
+        u64 cb[NINT];
+#pragma unroll
+        for (int w = 0; w < NINT; ++w) cb[w] = a.beta[(int64_t)bp * NINT + w];
+        const int end = a.col_loc[bp + 1];
+        for (int p0 = a.col_loc[bp]; p0 < end; p0 += 32) {
+          const int pos = p0 + lane;
+          bool hit = false;
+          u64 ca[NINT];
+          if (pos < end) {
+            const int ap = a.rows[pos];
+            int d = 0;
+#pragma unroll
+            for (int w = 0; w < NINT; ++w) {
+              ca[w] = a.alpha[(int64_t)ap * NINT + w];
+              d += popc64(my[w] ^ ca[w]);
+            }
+            hit = (d == 2);
+          }
+          const unsigned bal = __ballot_sync(0xffffffffu, hit);
+          const bool flip = hit && spin_flip<NINT>(my, ca, cb);
+          const unsigned sbal = __ballot_sync(0xffffffffu, flip);
+          if (FILL && hit) {
+            u64 J[2 * NINT];
+#pragma unroll
+            for (int w = 0; w < NINT; ++w) {
+              J[w] = ca[w];
+              J[NINT + w] = cb[w];
+            }
+            double s2;
+            const double v = h_double_ab<NINT>(a.t, my, J, &s2, nullptr, nullptr);
+            const int64_t o = out + cnt + __popc(bal & lt);
+            if (o < a.rowptr[k + 1]) {
+              a.colidx[o] = pos;
+              a.val64[o] = v;
+              a.val32[o] = (float)v;
+            } else {
+              atomicOr(a.err, 4);
+            }
+            if (flip) {
+              const int64_t so = sout + scnt + __popc(sbal & lt);
+              if (so < a.s2ptr[k + 1]) {
+                a.s2col[so] = pos;
+                a.s2val[so] = (float)s2;
+              } else {
+                atomicOr(a.err, 8);
+              }
+            }
+          }
+          cnt += __popc(bal);
+          scnt += __popc(sbal);
+        }
+      }
+    } else {
+      for (int t = a.sa_ptr[ai]; t < a.sa_ptr[ai + 1]; ++t) {
+        const int ap = a.sa_idx[t];
+        u64 ca[NINT];
+#pragma unroll
+        for (int w = 0; w < NINT; ++w) ca[w] = a.alpha[(int64_t)ap * NINT + w];
+        const int end = a.row_loc[ap + 1];
+        for (int q0 = a.row_loc[ap]; q0 < end; q0 += 32) {
+          const int q = q0 + lane;
+          bool hit = false;
+          u64 cb[NINT];
+          if (q < end) {
+            const int bp = a.t_cols[q];
+            int d = 0;
+#pragma unroll
+            for (int w = 0; w < NINT; ++w) {
+              cb[w] = a.beta[(int64_t)bp * NINT + w];
+              d += popc64(my[NINT + w] ^ cb[w]);
+            }
+            hit = (d == 2);
+          }
+          const unsigned bal = __ballot_sync(0xffffffffu, hit);
+          const bool flip = hit && spin_flip<NINT>(my, ca, cb);
+          const unsigned sbal = __ballot_sync(0xffffffffu, flip);
+          if (FILL && hit) {
+            u64 J[2 * NINT];
+#pragma unroll
+            for (int w = 0; w < NINT; ++w) {
+              J[w] = ca[w];
+              J[NINT + w] = cb[w];
+            }
+            double s2;
+            const double v = h_double_ab<NINT>(a.t, my, J, &s2, nullptr, nullptr);
+            const int64_t o = out + cnt + __popc(bal & lt);
+            const int jpos = a.t_order[q];
+            if (o < a.rowptr[k + 1]) {
+              a.colidx[o] = jpos;
+              a.val64[o] = v;
+              a.val32[o] = (float)v;
+            } else {
+              atomicOr(a.err, 4);
+            }
+            if (flip) {
+              const int64_t so = sout + scnt + __popc(sbal & lt);
+              if (so < a.s2ptr[k + 1]) {
+                a.s2col[so] = jpos;
+                a.s2val[so] = (float)s2;
+              } else {
+                atomicOr(a.err, 8);
+              }
+            }
+          }
+          cnt += __popc(bal);
+          scnt += __popc(sbal);
+        }
+      }
+    }
+    if (!FILL && lane == 0) {
+      a.cntC[k] = cnt;
+      a.cntS[k] = scnt;
+    }
+  }
+}
+
+__global__ void k_row_totals(const int* A, const int* B, const int* C, const int* S, int64_t* tot, int64_t* stot,
+                             int64_t N) {
+  for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k <= N; k += (int64_t)gridDim.x * blockDim.x) {
+    tot[k] = (k < N) ? (int64_t)A[k] + B[k] + C[k] : 0;
+    stot[k] = (k < N) ? (int64_t)S[k] : 0;
+  }
+}
+
+// H_II and <I|S+S-|I> in bilinear order (diag_H_mat_elem, slater_rules.irp.f:1869;
+// diag_S_mat_elem, s2.irp.f:1-30)
+template <int NINT>
+__global__ void k_diag(DevTables t, const u64* alpha, const u64* beta, const int* rows, const int* cols,
+                       double* hd, double* sd, float* hd32, int64_t N) {
+  for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < N; k += (int64_t)gridDim.x * blockDim.x) {
+    u64 det[2 * NINT];
+    const int ai = rows[k], bi = cols[k];
+#pragma unroll
+    for (int w = 0; w < NINT; ++w) {
+      det[w] = alpha[(int64_t)ai * NINT + w];
+      det[NINT + w] = beta[(int64_t)bi * NINT + w];
+    }
+    const double h = diag_h<NINT>(t, det);
+    hd[k] = h;
+    hd32[k] = (float)h;
+    sd[k] = diag_s<NINT>(det);
+  }
+}
+
+template <int NINT>
+int build_pairs_t(qpgpu_ctx* c) {
+  const int64_t N = c->N;
+  cudaStream_t st = c->stream;
+  BuildArgs a{};
+  a.t = c->tab;
+  a.N = N;
+  a.alpha = c->d_alpha;
+  a.beta = c->d_beta;
+  a.rows = c->d_rows;
+  a.cols = c->d_cols;
+  a.col_loc = c->d_col_loc;
+  a.t_order = c->d_t_order;
+  a.t_cols = c->d_t_cols;
+  a.row_loc = c->d_row_loc;
+  a.sa_ptr = c->d_sa_ptr;
+  a.sa_idx = c->d_sa_idx;
+  a.sb_ptr = c->d_sb_ptr;
+  a.sb_idx = c->d_sb_idx;
+  a.cost_a = c->d_cost_a;
+  a.cost_b = c->d_cost_b;
+  Scoped<int> cA, cB, cC, cS;
+  QP_CUDA(c, dev_alloc(&cA.p, N));
+  QP_CUDA(c, dev_alloc(&cB.p, N));
+  QP_CUDA(c, dev_alloc(&cC.p, N));
+  QP_CUDA(c, dev_alloc(&cS.p, N));
+  a.cntA = cA.p;
+  a.cntB = cB.p;
+  a.cntC = cC.p;
+  a.cntS = cS.p;
+  const unsigned gAB = nblocks(N, BLK);
+  const unsigned gC = nblocks(N * 32, BLK);
+  k_class_a<NINT, false><<<gAB, BLK, 0, st>>>(a);
+  k_class_b<NINT, false><<<gAB, BLK, 0, st>>>(a);
+  k_class_c<NINT, false><<<gC, BLK, 0, st>>>(a);
+  QP_CUDA(c, cudaGetLastError());
+  Scoped<int64_t> tot, stot;
+  QP_CUDA(c, dev_alloc(&tot.p, N + 1));
+  QP_CUDA(c, dev_alloc(&stot.p, N + 1));
+  k_row_totals<<<nblocks(N + 1, 256), 256, 0, st>>>(cA.p, cB.p, cC.p, cS.p, tot.p, stot.p, N);
+  QP_CUDA(c, dev_alloc(&c->d_rowptr, N + 1));
+  QP_CUDA(c, dev_alloc(&c->d_s2ptr, N + 1));
+  size_t tb = 0;
+  QP_CUDA(c, cub::DeviceScan::ExclusiveSum(nullptr, tb, tot.p, c->d_rowptr, (int)(N + 1), st));
+  Scoped<char> tmp;
+  QP_CUDA(c, dev_alloc(&tmp.p, tb));
+  QP_CUDA(c, cub::DeviceScan::ExclusiveSum(tmp.p, tb, tot.p, c->d_rowptr, (int)(N + 1), st));
+  QP_CUDA(c, cub::DeviceScan::ExclusiveSum(tmp.p, tb, stot.p, c->d_s2ptr, (int)(N + 1), st));
+  QP_CUDA(c, cudaMemcpyAsync(&c->P, c->d_rowptr + N, sizeof(int64_t), cudaMemcpyDeviceToHost, st));
+  QP_CUDA(c, cudaMemcpyAsync(&c->P_s2, c->d_s2ptr + N, sizeof(int64_t), cudaMemcpyDeviceToHost, st));
+  QP_CUDA(c, cudaStreamSynchronize(st));
+  const int64_t P = c->P, PS = c->P_s2;
+  if (dev_alloc(&c->d_colidx, P) != cudaSuccess || dev_alloc(&c->d_val64, P) != cudaSuccess ||
+      dev_alloc(&c->d_val32, P) != cudaSuccess || dev_alloc(&c->d_s2col, PS) != cudaSuccess ||
+      dev_alloc(&c->d_s2val, PS) != cudaSuccess) {
+    cudaGetLastError();
+    return qpgpu_fail(c, QPGPU_ERR_NOMEM,
+                      "not enough device memory for " + std::to_string(P) + " connected pairs");
+  }
+  a.rowptr = c->d_rowptr;
+  a.colidx = c->d_colidx;
+  a.val64 = c->d_val64;
+  a.val32 = c->d_val32;
+  a.s2ptr = c->d_s2ptr;
+  a.s2col = c->d_s2col;
+  a.s2val = c->d_s2val;
+  Scoped<int> err;
+  QP_CUDA(c, dev_alloc(&err.p, 1));
+  QP_CUDA(c, cudaMemsetAsync(err.p, 0, sizeof(int), st));
+  a.err = err.p;
+  k_class_a<NINT, true><<<gAB, BLK, 0, st>>>(a);
+  k_class_b<NINT, true><<<gAB, BLK, 0, st>>>(a);
+  k_class_c<NINT, true><<<gC, BLK, 0, st>>>(a);
+  QP_CUDA(c, cudaGetLastError());
+  int herr = 0;
+  QP_CUDA(c, cudaMemcpyAsync(&herr, err.p, sizeof(int), cudaMemcpyDeviceToHost, st));
+  QP_CUDA(c, cudaStreamSynchronize(st));
+  if (herr) return qpgpu_fail(c, QPGPU_ERR_STATE, "pair fill disagrees with pair count (" + std::to_string(herr) + ")");
+  QP_CUDA(c, dev_alloc(&c->d_hdiag, N));
+  QP_CUDA(c, dev_alloc(&c->d_sdiag, N));
+  QP_CUDA(c, dev_alloc(&c->d_hdiag32, N));
+  k_diag<NINT><<<nblocks(N, 256), 256, 0, st>>>(c->tab, c->d_alpha, c->d_beta, c->d_rows, c->d_cols, c->d_hdiag,
+                                                 c->d_sdiag, c->d_hdiag32, N);
+  QP_CUDA(c, cudaGetLastError());
+  QP_CUDA(c, cudaStreamSynchronize(st));
+  return 0;
+}
+
+}  // namespace
+
+void qp_free_pairs(qpgpu_ctx* c) {
+  void** ps[] = {(void**)&c->d_rowptr, (void**)&c->d_colidx, (void**)&c->d_val64, (void**)&c->d_val32,
+                 (void**)&c->d_s2ptr, (void**)&c->d_s2col, (void**)&c->d_s2val, (void**)&c->d_hdiag,
+                 (void**)&c->d_sdiag, (void**)&c->d_hdiag32};
+  for (auto p : ps) {
+    dev_free(*p);
+    *p = nullptr;
+  }
+  c->have_pairs = false;
+  c->P = c->P_s2 = 0;
+}
+
+int qp_build_pairs(qpgpu_ctx* c) {
+  if (c->nint == 1) return build_pairs_t<1>(c);
+  if (c->nint == 2) return build_pairs_t<2>(c);
+  return qpgpu_fail(c, QPGPU_ERR_ARG, "n_int > 2 is not supported");
+}

@@ -1,0 +1,367 @@
+// Sigma application v = H u, s = S^2 u over the stored connected pairs.
+//
+// The reference computes every matrix element again at each call
+// (src/Davidson/u0Hu0.irp.f:177-444); here they are built once per
+// determinant set and sigma is a row-owner gather: each row is owned by one
+// warp (rows longer than CHUNK pairs are split over several warps whose
+// partial sums are added in a fixed order), so there are no atomics and the
+// result is deterministic.  u is laid out (N_det, N_st) with states fastest,
+// as u_t(N_st, N_det) in the reference (:27-41), so the N_st coefficients of a
+// connected determinant J are one contiguous load.
+#include "qpgpu_internal.cuh"
+
+namespace {
+
+constexpr int SBLK = 256;
+
+struct SigArgs {
+  int64_t N;
+  const int64_t* rowptr;
+  const int* colidx;
+  const double* val64;
+  const float* val32;
+  const int64_t* s2ptr;
+  const int* s2col;
+  const float* s2val;
+  const double* hdiag;
+  const double* sdiag;
+  const int* item_row;
+  const int* item_sub;
+  const int* row_nitems;
+  int64_t n_items;
+  const double* u;   // (N, NST) FP64
+  const float* u32;  // (N, NST) FP32 (precision FP32)
+  double* v;
+  double* s;
+  double* pv;  // partial sums (n_items, NST)
+  double* ps;
+  int row_lo, row_hi;  // rows [row_lo, row_hi) are written (range variant)
+  int row_step, row_first;
+};
+
+__device__ __forceinline__ double warp_sum(double x) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) x += __shfl_xor_sync(0xffffffffu, x, o);
+  return x;
+}
+
+__device__ __forceinline__ bool row_selected(const SigArgs& a, int k) {
+  if (k < a.row_lo || k >= a.row_hi) return false;
+  return ((k - a.row_first) % a.row_step) == 0;
+}
+
+template <int NST>
+__global__ void __launch_bounds__(SBLK) k_sigma64(SigArgs a) {
+  const int lane = threadIdx.x & 31;
+  const int64_t warp = ((int64_t)blockIdx.x * SBLK + threadIdx.x) >> 5;
+  const int64_t nwarp = ((int64_t)gridDim.x * SBLK) >> 5;
+  for (int64_t it = warp; it < a.n_items; it += nwarp) {
+    const int k = a.item_row[it];
+    if (!row_selected(a, k)) continue;
+    const int j = a.item_sub[it];
+    const int64_t rb = a.rowptr[k], re = a.rowptr[k + 1];
+    const int64_t beg = rb + (int64_t)j * QP_SIGMA_CHUNK;
+    const int64_t end = min(beg + (int64_t)QP_SIGMA_CHUNK, re);
+    double acc[NST], sacc[NST];
+#pragma unroll
+    for (int st = 0; st < NST; ++st) acc[st] = sacc[st] = 0.0;
+    for (int64_t e = beg + lane; e < end; e += 32) {
+      const int col = __ldg(&a.colidx[e]);
+      const double hv = __ldg(&a.val64[e]);
+      const double* uj = a.u + (int64_t)col * NST;
+#pragma unroll
+      for (int st = 0; st < NST; ++st) acc[st] = fma(hv, __ldg(&uj[st]), acc[st]);
+    }
+    if (j == 0) {
+      const int64_t sb = a.s2ptr[k], se = a.s2ptr[k + 1];
+      for (int64_t e = sb + lane; e < se; e += 32) {
+        const int col = __ldg(&a.s2col[e]);
+        const double sv = (double)__ldg(&a.s2val[e]);
+        const double* uj = a.u + (int64_t)col * NST;
+#pragma unroll
+        for (int st = 0; st < NST; ++st) sacc[st] = fma(sv, __ldg(&uj[st]), sacc[st]);
+      }
+    }
+#pragma unroll
+    for (int st = 0; st < NST; ++st) {
+      acc[st] = warp_sum(acc[st]);
+      sacc[st] = warp_sum(sacc[st]);
+    }
+    if (a.row_nitems[k] == 1) {
+      if (lane < NST) {
+        double av = 0.0, as = 0.0, uk = a.u[(int64_t)k * NST + lane];
+#pragma unroll
+        for (int st = 0; st < NST; ++st)
+          if (st == lane) { av = acc[st]; as = sacc[st]; }
+        a.v[(int64_t)k * NST + lane] = av + a.hdiag[k] * uk;
+        a.s[(int64_t)k * NST + lane] = as + a.sdiag[k] * uk;
+      }
+    } else if (lane < NST) {
+      double av = 0.0, as = 0.0;
+#pragma unroll
+      for (int st = 0; st < NST; ++st)
+        if (st == lane) { av = acc[st]; as = sacc[st]; }
+      a.pv[it * NST + lane] = av;
+      a.ps[it * NST + lane] = as;
+    }
+  }
+}
+
+// FP32 matrix elements x FP32 coefficients, Kahan-compensated per lane; lane
+// partials are combined in FP64 and the FP64 diagonal term is added.
+template <int NST>
+__global__ void __launch_bounds__(SBLK) k_sigma32(SigArgs a) {
+  const int lane = threadIdx.x & 31;
+  const int64_t warp = ((int64_t)blockIdx.x * SBLK + threadIdx.x) >> 5;
+  const int64_t nwarp = ((int64_t)gridDim.x * SBLK) >> 5;
+  for (int64_t it = warp; it < a.n_items; it += nwarp) {
+    const int k = a.item_row[it];
+    if (!row_selected(a, k)) continue;
+    const int j = a.item_sub[it];
+    const int64_t rb = a.rowptr[k], re = a.rowptr[k + 1];
+    const int64_t beg = rb + (int64_t)j * QP_SIGMA_CHUNK;
+    const int64_t end = min(beg + (int64_t)QP_SIGMA_CHUNK, re);
+    float sum[NST], cmp[NST];
+    double acc[NST], sacc[NST];
+#pragma unroll
+    for (int st = 0; st < NST; ++st) sum[st] = cmp[st] = 0.f;
+    for (int64_t e = beg + lane; e < end; e += 32) {
+      const int col = __ldg(&a.colidx[e]);
+      const float hv = __ldg(&a.val32[e]);
+      const float* uj = a.u32 + (int64_t)col * NST;
+#pragma unroll
+      for (int st = 0; st < NST; ++st) {
+        const float y = __fmaf_rn(hv, __ldg(&uj[st]), -cmp[st]);
+        const float t = __fadd_rn(sum[st], y);
+        cmp[st] = __fsub_rn(__fsub_rn(t, sum[st]), y);
+        sum[st] = t;
+      }
+    }
+#pragma unroll
+    for (int st = 0; st < NST; ++st) {
+      acc[st] = (double)sum[st] - (double)cmp[st];
+      sacc[st] = 0.0;
+    }
+    if (j == 0) {
+      const int64_t sb = a.s2ptr[k], se = a.s2ptr[k + 1];
+      for (int64_t e = sb + lane; e < se; e += 32) {
+        const int col = __ldg(&a.s2col[e]);
+        const double sv = (double)__ldg(&a.s2val[e]);
+        const float* uj = a.u32 + (int64_t)col * NST;
+#pragma unroll
+        for (int st = 0; st < NST; ++st) sacc[st] = fma(sv, (double)__ldg(&uj[st]), sacc[st]);
+      }
+    }
+#pragma unroll
+    for (int st = 0; st < NST; ++st) {
+      acc[st] = warp_sum(acc[st]);
+      sacc[st] = warp_sum(sacc[st]);
+    }
+    if (a.row_nitems[k] == 1) {
+      if (lane < NST) {
+        double av = 0.0, as = 0.0, uk = a.u[(int64_t)k * NST + lane];
+#pragma unroll
+        for (int st = 0; st < NST; ++st)
+          if (st == lane) { av = acc[st]; as = sacc[st]; }
+        a.v[(int64_t)k * NST + lane] = av + a.hdiag[k] * uk;
+        a.s[(int64_t)k * NST + lane] = as + a.sdiag[k] * uk;
+      }
+    } else if (lane < NST) {
+      double av = 0.0, as = 0.0;
+#pragma unroll
+      for (int st = 0; st < NST; ++st)
+        if (st == lane) { av = acc[st]; as = sacc[st]; }
+      a.pv[it * NST + lane] = av;
+      a.ps[it * NST + lane] = as;
+    }
+  }
+}
+
+// rows split over several items: add the partials in item order
+__global__ void k_sigma_combine(SigArgs a, const int* multi_rows, const int* row_item0, int n_multi, int nst) {
+  for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < (int64_t)n_multi * nst;
+       t += (int64_t)gridDim.x * blockDim.x) {
+    const int k = multi_rows[t / nst];
+    const int st = (int)(t % nst);
+    if (!row_selected(a, k)) continue;
+    const int i0 = row_item0[k], ni = a.row_nitems[k];
+    double av = 0.0, as = 0.0;
+    for (int i = 0; i < ni; ++i) {
+      av += a.pv[(int64_t)(i0 + i) * nst + st];
+      as += a.ps[(int64_t)(i0 + i) * nst + st];
+    }
+    const double uk = a.u[(int64_t)k * nst + st];
+    a.v[(int64_t)k * nst + st] = av + a.hdiag[k] * uk;
+    a.s[(int64_t)k * nst + st] = as + a.sdiag[k] * uk;
+  }
+}
+
+// ---- work items -----------------------------------------------------------
+__global__ void k_row_nitems(const int64_t* rowptr, int* nit, int64_t N) {
+  for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < N; k += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t nnz = rowptr[k + 1] - rowptr[k];
+    nit[k] = (int)max((int64_t)1, (nnz + QP_SIGMA_CHUNK - 1) / QP_SIGMA_CHUNK);
+  }
+}
+
+__global__ void k_fill_items(const int* nit, const int* item0, int* item_row, int* item_sub, int64_t N) {
+  for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < N; k += (int64_t)gridDim.x * blockDim.x)
+    for (int j = 0; j < nit[k]; ++j) {
+      item_row[item0[k] + j] = (int)k;
+      item_sub[item0[k] + j] = j;
+    }
+}
+
+template <class T>
+__global__ void k_to_bilinear(const T* u0, int64_t ld, const int* order, double* ut, float* ut32, int nst,
+                              int64_t N) {
+  for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < N * nst; t += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t p = t / nst;
+    const int st = (int)(t % nst);
+    const double x = (double)u0[(int64_t)st * ld + order[p]];
+    if (ut) ut[t] = x;
+    if (ut32) ut32[t] = (float)x;
+  }
+}
+
+__global__ void k_from_bilinear(const double* vt, int64_t ld, const int* order, double* v0, int nst, int64_t N) {
+  for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < N * nst; t += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t p = t / nst;
+    const int st = (int)(t % nst);
+    v0[(int64_t)st * ld + order[p]] = vt[t];
+  }
+}
+
+__global__ void k_to_float(const double* x, float* y, int64_t n) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+    y[i] = (float)x[i];
+}
+
+inline unsigned gsz(int64_t n, int tpb) {
+  int64_t g = (n + tpb - 1) / tpb;
+  if (g < 1) g = 1;
+  if (g > 65535LL * 32) g = 65535LL * 32;
+  return (unsigned)g;
+}
+
+template <int NST>
+void launch_sigma(const SigArgs& a, int precision, unsigned grid, cudaStream_t st) {
+  if (precision == QPGPU_FP32)
+    k_sigma32<NST><<<grid, SBLK, 0, st>>>(a);
+  else
+    k_sigma64<NST><<<grid, SBLK, 0, st>>>(a);
+}
+
+}  // namespace
+
+// Work items of the sigma kernels (one per chunk of a row), built after the pairs.
+int qp_build_sigma_items(qpgpu_ctx* c, SigmaItems* it) {
+  const int64_t N = c->N;
+  cudaStream_t st = c->stream;
+  it->free_all();
+  QP_CUDA(c, dev_alloc(&it->row_nitems, N + 1));
+  QP_CUDA(c, dev_alloc(&it->row_item0, N + 1));
+  k_row_nitems<<<gsz(N, 256), 256, 0, st>>>(c->d_rowptr, it->row_nitems, N);
+  QP_CUDA(c, cudaMemsetAsync(it->row_nitems + N, 0, sizeof(int), st));
+  std::vector<int> nit(N);
+  QP_CUDA(c, cudaMemcpyAsync(nit.data(), it->row_nitems, N * sizeof(int), cudaMemcpyDeviceToHost, st));
+  QP_CUDA(c, cudaStreamSynchronize(st));
+  std::vector<int> item0(N + 1);
+  std::vector<int> multi;
+  int64_t acc = 0;
+  for (int64_t k = 0; k < N; ++k) {
+    item0[k] = (int)acc;
+    acc += nit[k];
+    if (nit[k] > 1) multi.push_back((int)k);
+  }
+  item0[N] = (int)acc;
+  it->n_items = acc;
+  it->n_multi = (int)multi.size();
+  QP_CUDA(c, cudaMemcpyAsync(it->row_item0, item0.data(), (N + 1) * sizeof(int), cudaMemcpyHostToDevice, st));
+  QP_CUDA(c, dev_alloc(&it->item_row, acc));
+  QP_CUDA(c, dev_alloc(&it->item_sub, acc));
+  QP_CUDA(c, dev_alloc(&it->multi_rows, multi.size() + 1));
+  if (!multi.empty())
+    QP_CUDA(c, cudaMemcpyAsync(it->multi_rows, multi.data(), multi.size() * sizeof(int), cudaMemcpyHostToDevice, st));
+  k_fill_items<<<gsz(N, 256), 256, 0, st>>>(it->row_nitems, it->row_item0, it->item_row, it->item_sub, N);
+  QP_CUDA(c, cudaGetLastError());
+  QP_CUDA(c, cudaStreamSynchronize(st));
+  return 0;
+}
+
+// Partial-sum buffers sized for nst states.
+static int ensure_partials(qpgpu_ctx* c, SigmaItems* it, int nst) {
+  const size_t need = (size_t)it->n_items * nst;
+  if (it->partial_cap >= need) return 0;
+  dev_free(it->pv);
+  dev_free(it->ps);
+  it->pv = it->ps = nullptr;
+  it->partial_cap = 0;
+  QP_CUDA(c, dev_alloc(&it->pv, need));
+  QP_CUDA(c, dev_alloc(&it->ps, need));
+  it->partial_cap = need;
+  return 0;
+}
+
+int qp_sigma_launch(qpgpu_ctx* c, SigmaItems* it, double* v, double* s, const double* u, const float* u32, int nst,
+                    int precision, cudaStream_t st, int row_lo, int row_hi, int row_first, int row_step) {
+  if (nst < 1 || nst > 8) return qpgpu_fail(c, QPGPU_ERR_ARG, "n_st must be in 1..8 per sigma block");
+  if (precision == QPGPU_FP32 && !u32) return qpgpu_fail(c, QPGPU_ERR_ARG, "FP32 sigma needs u_t32");
+  int rc = ensure_partials(c, it, nst);
+  if (rc) return rc;
+  SigArgs a{};
+  a.N = c->N;
+  a.rowptr = c->d_rowptr;
+  a.colidx = c->d_colidx;
+  a.val64 = c->d_val64;
+  a.val32 = c->d_val32;
+  a.s2ptr = c->d_s2ptr;
+  a.s2col = c->d_s2col;
+  a.s2val = c->d_s2val;
+  a.hdiag = c->d_hdiag;
+  a.sdiag = c->d_sdiag;
+  a.item_row = it->item_row;
+  a.item_sub = it->item_sub;
+  a.row_nitems = it->row_nitems;
+  a.n_items = it->n_items;
+  a.u = u;
+  a.u32 = u32;
+  a.v = v;
+  a.s = s;
+  a.pv = it->pv;
+  a.ps = it->ps;
+  a.row_lo = row_lo;
+  a.row_hi = row_hi;
+  a.row_first = row_first;
+  a.row_step = row_step;
+  const unsigned grid = gsz(it->n_items * 32, SBLK);
+  switch (nst) {
+    case 1: launch_sigma<1>(a, precision, grid, st); break;
+    case 2: launch_sigma<2>(a, precision, grid, st); break;
+    case 3: launch_sigma<3>(a, precision, grid, st); break;
+    case 4: launch_sigma<4>(a, precision, grid, st); break;
+    case 5: launch_sigma<5>(a, precision, grid, st); break;
+    case 6: launch_sigma<6>(a, precision, grid, st); break;
+    case 7: launch_sigma<7>(a, precision, grid, st); break;
+    default: launch_sigma<8>(a, precision, grid, st); break;
+  }
+  if (it->n_multi > 0)
+    k_sigma_combine<<<gsz((int64_t)it->n_multi * nst, 256), 256, 0, st>>>(a, it->multi_rows, it->row_item0,
+                                                                         it->n_multi, nst);
+  QP_CUDA(c, cudaGetLastError());
+  return 0;
+}
+
+void qp_to_bilinear(const double* u0, int64_t ld, const int* order, double* ut, float* ut32, int nst, int64_t N,
+                    cudaStream_t st) {
+  k_to_bilinear<double><<<gsz(N * nst, 256), 256, 0, st>>>(u0, ld, order, ut, ut32, nst, N);
+}
+
+void qp_from_bilinear(const double* vt, int64_t ld, const int* order, double* v0, int nst, int64_t N,
+                      cudaStream_t st) {
+  k_from_bilinear<<<gsz(N * nst, 256), 256, 0, st>>>(vt, ld, order, v0, nst, N);
+}
+
+void qp_to_float(const double* x, float* y, int64_t n, cudaStream_t st) {
+  k_to_float<<<gsz(n, 256), 256, 0, st>>>(x, y, n);
+}

@@ -1,0 +1,143 @@
+"""Host-side mirror of Quantum Package's sigma interface over libqpgpu.
+
+The reference keeps the determinant set and integrals in IRPF90 providers and
+exposes ``H_S2_u_0_nstates_openmp(v_0, s_0, u_0, N_st, sze)``
+(src/Davidson/u0Hu0.irp.f:15-66) and its range variant
+``H_S2_u_0_nstates_openmp_work(v_t, s_t, u_t, N_st, sze, istart, iend, ishift,
+istep)`` (:69-96).  ``Wavefunction`` plays the role of those providers: it
+holds a device context (integral tables, bilinear index, connected pairs) and
+offers the same entry points with the same argument meaning.
+
+Array conventions: a Fortran array ``u_0(sze, N_st)`` is a C-contiguous numpy
+array of shape ``(N_st, sze)``; ``u_t(N_st, N_det)`` is shape ``(N_det, N_st)``.
+"""
+from __future__ import annotations
+
+import ctypes as C
+
+import numpy as np
+
+from . import _lib
+from ._lib import FP32, FP64, check
+
+
+def _p(a):
+    return C.c_void_p(a.ctypes.data) if a is not None else None
+
+
+class Wavefunction:
+    """Providers of one orbital space and determinant set, on the GPU."""
+
+    def __init__(self, n_mo: int, n_alpha: int, n_beta: int, h=None, eri=None, psi_det=None):
+        L = _lib.load()
+        self.n_mo, self.n_alpha, self.n_beta = n_mo, n_alpha, n_beta
+        self.n_int = (n_mo - 1) // 64 + 1
+        h_ = C.c_void_p()
+        rc = L.qpgpu_create(n_mo, n_alpha, n_beta, self.n_int, C.byref(h_))
+        if rc != 0:
+            raise _lib.QPGPUError(rc, "qpgpu_create failed (device or arguments)")
+        self._ctx = h_
+        self.n_det = 0
+        if h is not None:
+            self.set_integrals(h, eri)
+        if psi_det is not None:
+            self.set_dets(psi_det)
+
+    @classmethod
+    def from_problem(cls, prob):
+        return cls(prob.n_mo, prob.n_alpha, prob.n_beta, prob.ints.h, prob.ints.eri, prob.dets)
+
+    def close(self):
+        if getattr(self, "_ctx", None):
+            _lib.load().qpgpu_destroy(self._ctx)
+            self._ctx = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    @property
+    def ctx(self):
+        return self._ctx
+
+    def set_integrals(self, h, eri):
+        hf = np.ascontiguousarray(np.asarray(h, dtype=np.float64).T)  # column-major h(i,j)
+        e = np.ascontiguousarray(eri, dtype=np.float64)
+        check(_lib.load().qpgpu_set_integrals(self._ctx, _p(hf), _p(e)), self._ctx)
+
+    def set_dets(self, psi_det):
+        d = np.ascontiguousarray(psi_det, dtype=np.uint64)
+        if d.ndim != 3 or d.shape[1] != 2 or d.shape[2] != self.n_int:
+            raise ValueError("psi_det must have shape (N_det, 2, N_int)")
+        check(_lib.load().qpgpu_set_dets(self._ctx, _p(d), d.shape[0]), self._ctx)
+        self.n_det = d.shape[0]
+
+    def info(self) -> dict:
+        i = _lib.Info()
+        check(_lib.load().qpgpu_get_info(self._ctx, C.byref(i)), self._ctx)
+        return {f: getattr(i, f) for f, _ in i._fields_}
+
+    # --- sigma ---------------------------------------------------------
+    def H_S2_u_0_nstates_openmp(self, u_0):
+        """v_0 = H u_0, s_0 = S^2 u_0 (no S_z(S_z-1) shift); u_0: (N_st, sze) -> (v_0, s_0)."""
+        u = np.ascontiguousarray(np.atleast_2d(u_0), dtype=np.float64)
+        n_st, ld = u.shape
+        v = np.zeros_like(u)
+        s = np.zeros_like(u)
+        check(_lib.load().qpgpu_h_s2_u0(self._ctx, _p(v), _p(s), _p(u), n_st, ld), self._ctx)
+        return v, s
+
+    def H_S2_u_0_nstates_openmp_work(self, u_t, istart, iend, ishift=0, istep=1, v_t=None, s_t=None):
+        """Range variant in bilinear order; u_t: (N_det, N_st).  Rows outside the range are untouched."""
+        u = np.ascontiguousarray(u_t, dtype=np.float64)
+        v = np.zeros_like(u) if v_t is None else v_t
+        s = np.zeros_like(u) if s_t is None else s_t
+        check(_lib.load().qpgpu_h_s2_u0_work(self._ctx, _p(v), _p(s), _p(u), u.shape[1], istart, iend, ishift,
+                                             istep), self._ctx)
+        return v, s
+
+    def h_s2_u0_device(self, v0, s0, u0, precision=FP64, stream=None):
+        """torch CUDA tensors (N_st, ld) float64; asynchronous on `stream` (torch stream or None)."""
+        n_st, ld = u0.shape
+        st = C.c_void_p(stream.cuda_stream) if stream is not None else None
+        check(_lib.load().qpgpu_h_s2_u0_device(self._ctx, C.c_void_p(v0.data_ptr()), C.c_void_p(s0.data_ptr()),
+                                               C.c_void_p(u0.data_ptr()), n_st, ld, precision, st), self._ctx)
+
+    def sigma_bilinear(self, v_t, s_t, u_t, u_t32=None, precision=FP64, stream=None):
+        """Internal layout: torch CUDA tensors (N_det, N_st), bilinear order."""
+        st = C.c_void_p(stream.cuda_stream) if stream is not None else None
+        p32 = C.c_void_p(u_t32.data_ptr()) if u_t32 is not None else None
+        check(_lib.load().qpgpu_sigma_bilinear(self._ctx, C.c_void_p(v_t.data_ptr()), C.c_void_p(s_t.data_ptr()),
+                                               C.c_void_p(u_t.data_ptr()), p32, u_t.shape[1], precision, st),
+              self._ctx)
+
+    def bilinear_order(self):
+        o = np.empty(self.n_det, np.int32)
+        check(_lib.load().qpgpu_bilinear_order(self._ctx, _p(o)), self._ctx)
+        return o
+
+    def diag(self):
+        """(H_jj, <I|S+S-|I>) in psi_det order."""
+        h = np.empty(self.n_det)
+        s = np.empty(self.n_det)
+        check(_lib.load().qpgpu_diag(self._ctx, _p(h), _p(s)), self._ctx)
+        return h, s
+
+    def connected_pairs(self):
+        """Pairs sorted by (I, J): I, J (0-based psi_det), class, phase, exc (P,4), hij."""
+        L = _lib.load()
+        n = C.c_int64()
+        check(L.qpgpu_connected_pairs(self._ctx, C.byref(n), None, None, None, None, None, None, 0), self._ctx)
+        P = n.value
+        I = np.empty(P, np.int32)
+        J = np.empty(P, np.int32)
+        cls = np.empty(P, np.int8)
+        ph = np.empty(P, np.int8)
+        exc = np.empty((P, 4), np.int16)
+        hij = np.empty(P)
+        check(L.qpgpu_connected_pairs(self._ctx, C.byref(n), _p(I), _p(J), _p(cls), _p(ph), _p(exc), _p(hij), P),
+              self._ctx)
+        o = np.lexsort((J, I))
+        return dict(I=I[o], J=J[o], cls=cls[o], phase=ph[o], exc=exc[o], hij=hij[o])

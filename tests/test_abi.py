@@ -1,0 +1,21 @@
+"""The C-ABI library builds for sm_103a, loads and exports every declared symbol (no GPU needed)."""
+import ctypes
+
+from quantum_package_gb300 import _lib
+
+
+def test_library_exports_every_declared_symbol():
+    L = _lib.load()
+    names = _lib.declared_symbols()
+    assert "qpgpu_h_s2_u0" in names and "qpgpu_set_dets" in names
+    missing = [n for n in names if not hasattr(L, n)]
+    assert not missing, missing
+
+
+def test_create_rejects_bad_shapes_without_gpu_work():
+    L = _lib.load()
+    h = ctypes.c_void_p()
+    assert L.qpgpu_create(300, 2, 2, 5, ctypes.byref(h)) == -1      # n_mo too large
+    assert L.qpgpu_create(80, 14, 14, 1, ctypes.byref(h)) == -1     # wrong n_int
+    assert L.qpgpu_create(80, 10, 12, 2, ctypes.byref(h)) == -1     # n_alpha < n_beta
+    assert L.qpgpu_destroy(None) == -1
