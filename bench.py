@@ -1,0 +1,328 @@
+"""Benchmark of the Davidson sigma path (sigma = H.C and S^2.C) on one GB300.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference] [--n-det N]
+
+Workload: 14 alpha + 14 beta electrons in 80 MOs (N_int = 2), 1e6 seeded
+determinants (aufbau reference + random <=4-fold excitations), seeded integrals
+(h_pp ~ U[-2,2] sorted, h_pq ~ N(0,0.02), (pq|rs) = sum_k L^k_pq L^k_rs with 120
+factors L ~ N(0,0.05)), 4 states.  One step is one sigma application on all
+N_det rows for the 4 states.  The determinant set's connectivity and matrix
+elements are built once (qpgpu_set_dets, the provider rebuild after TOUCH
+psi_det) outside the timed region and reported as `setup_s`; Davidson calls
+sigma ~10-30 times per determinant set.
+
+value      FP64 sigma on device-resident vectors (kernel path), det*state/s
+e2e        FP64 sigma through qpgpu_h_s2_u0 with host (pinned) buffers,
+           host<->device copies inside the timed region
+sigma_fp32 FP32 matrix elements x FP32 coefficients with Kahan sums
+roofline   dominant kernel k_sigma64: algorithmic bytes per launch
+           B = N*N_st*8*3 + N*(2*N_int*8+12) + P*N_st*8 over its CUDA-event time
+cpu_baseline  the CPU oracle (C++ restatement of H_S2_u_0_nstates_openmp_work,
+           OpenMP, all host threads) on a strided row sample of the same workload
+--impl reference: that CPU path alone, as the reference arm.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+import numpy as np  # noqa: E402
+
+METRIC = "Davidson time-to-E (≤1e-6 Ha vs FP64) & σ det·states/s: mixed+learned vs plain"
+UNIT = "det*state/s"
+N_STATES = 4
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--n-det", type=int, default=1_000_000)
+    ap.add_argument("--cpu-sample-step", type=int, default=250,
+                    help="row stride of the CPU-oracle sample (1/step of the rows)")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    return ap.parse_args()
+
+
+def dist_env():
+    return int(os.environ.get("RANK", 0)), int(os.environ.get("WORLD_SIZE", 1)), int(os.environ.get("LOCAL_RANK", 0))
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled while the timed region runs."""
+
+    Q = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index=0):
+        self.index = index
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.Q}", "--format=csv,noheader,nounits",
+                 "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except (OSError, FileNotFoundError):
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            f = [x.strip() for x in ln.split(",")]
+            if len(f) < 7:
+                continue
+            try:
+                sm.append(float(f[0]))
+                mx = float(f[1])
+            except ValueError:
+                continue
+            for nm, v in zip(names, f[3:7]):
+                if v.lower().startswith("active"):
+                    reasons.add(nm)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": mx, "reasons": ["unsampled"]}
+        return {"sm_mhz": float(np.median(sm)), "sm_max_mhz": mx, "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def measured_peak_hbm():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        with open(p) as f:
+            return float(json.load(f)["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def profiled_traffic(N, P):
+    """dram bytes per k_sigma64 launch from the committed ncu summary, scaled to this workload."""
+    p = os.path.join(ROOT, "profiles", "sigma_fp64_ncu.json")
+    if not os.path.exists(p):
+        return None, None
+    with open(p) as f:
+        d = json.load(f)
+    try:
+        scale = P / float(d["n_pairs"])
+        return float(d["dram_bytes_per_launch"]) * scale, d.get("note")
+    except (KeyError, ZeroDivisionError):
+        return None, None
+
+
+def cpu_sample(prob, step, nst=N_STATES, repeat=1):
+    """CPU oracle sigma on rows 1, 1+step, ...: returns (det*state/s, seconds, rows, threads)."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    from oracle import Oracle, num_threads
+    o = Oracle.from_problem(prob)
+    from quantum_package_gb300 import generate as G
+    u_t = np.ascontiguousarray(G.random_coefficients(prob.n_det, nst, prob.seed).T)
+    rows = len(range(0, prob.n_det, step))
+    best = None
+    for _ in range(repeat):
+        t = time.perf_counter()
+        o.h_s2_u0_work(u_t, 1, prob.n_det, 0, step)
+        dt = time.perf_counter() - t
+        best = dt if best is None else min(best, dt)
+    return rows * nst / best, best, rows, num_threads(), o
+
+
+def run_reference(args):
+    rank, world, _ = dist_env()
+    if rank != 0:
+        return 0
+    from quantum_package_gb300 import generate as G
+    prob = G.make_problem(2, n_det=args.n_det, n_states=N_STATES)
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    from oracle import Oracle, num_threads
+    o = Oracle.from_problem(prob)
+    u_t = np.ascontiguousarray(G.random_coefficients(prob.n_det, N_STATES, prob.seed).T)
+    step = args.cpu_sample_step
+    rows = len(range(0, prob.n_det, step))
+    for _ in range(args.warmup):
+        o.h_s2_u0_work(u_t, 1, prob.n_det, 0, step)
+    t = time.perf_counter()
+    for _ in range(args.steps):
+        o.h_s2_u0_work(u_t, 1, prob.n_det, 0, step)
+    dt = time.perf_counter() - t
+    val = rows * N_STATES * args.steps / dt
+    sample = f"rows 1+{step}k of {prob.n_det} ({rows} rows, {N_STATES} states) per step"
+    line = {
+        "impl": "reference", "metric": METRIC, "value": val, "unit": UNIT, "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": dt / args.steps * 1e3,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": workload_config(prob),
+        "cpu_baseline": {"value": val, "unit": UNIT, "cores": num_threads(), "kind": "port", "sample": sample},
+        "e2e": {"value": val, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "note": "CPU oracle (C++ FP64 restatement of u0Hu0.irp.f:97-448, OpenMP dynamic,64); the Fortran "
+                "reference cannot be compiled here (no gfortran/irpf90)",
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def workload_config(prob):
+    return {"workload": "sigma H.C+S2.C, 14a+14b in 80 MOs (N_int=2), 1e6 seeded dets, 4 states",
+            "n_det": prob.n_det, "n_mo": prob.n_mo, "n_alpha": prob.n_alpha, "n_beta": prob.n_beta,
+            "n_states": N_STATES, "seed": prob.seed,
+            "l2": "inputs larger than L2 (stored pairs ~12 GB FP64 per sigma)"}
+
+
+def run_ours(args):
+    import torch
+    rank, world, local = dist_env()
+    torch.cuda.set_device(local)
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
+    from quantum_package_gb300 import FP32, FP64
+    from quantum_package_gb300 import _lib
+    from quantum_package_gb300 import generate as G
+    from quantum_package_gb300.sigma import Wavefunction, stream_handle
+
+    prob = G.make_problem(2, n_det=args.n_det, n_states=N_STATES)
+    N = prob.n_det
+    # CPU baseline before any GPU work (oracle threads)
+    cpu = None
+    if rank == 0 and not args.no_cpu_baseline:
+        val, sec, rows, thr, _ = cpu_sample(prob, args.cpu_sample_step)
+        cpu = {"value": val, "unit": UNIT, "cores": thr, "kind": "port",
+               "sample": f"rows 1+{args.cpu_sample_step}k of {N} ({rows} rows, {N_STATES} states), {sec:.1f} s"}
+
+    wf = Wavefunction.from_problem(prob)
+    info = wf.info()
+    P = info["n_pairs"]
+    dev = torch.device("cuda", local)
+    stream = torch.cuda.Stream(device=dev)
+    order = torch.from_numpy(wf.bilinear_order().astype(np.int64)).to(dev)
+    u0 = torch.from_numpy(G.random_coefficients(N, N_STATES, prob.seed)).to(dev)
+    ut = u0[:, order].T.contiguous()
+    ut32 = ut.float()
+    v = torch.empty_like(ut)
+    s = torch.empty_like(ut)
+    launches_per_sigma = 1 + (1 if info["n_split_rows"] > 0 else 0)
+
+    def timed(prec, steps, warm):
+        with torch.cuda.stream(stream):
+            for _ in range(warm):
+                wf.sigma_bilinear(v, s, ut, ut32, prec, stream)
+            stream.synchronize()
+            if world > 1:
+                torch.distributed.barrier()
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            for _ in range(steps):
+                wf.sigma_bilinear(v, s, ut, ut32, prec, stream)
+            e1.record(stream)
+            stream.synchronize()
+        return e0.elapsed_time(e1) / steps
+
+    with ClockSampler(local) as clk:
+        ms64 = timed(FP64, args.steps, args.warmup)
+    ms32 = timed(FP32, args.steps, args.warmup)
+    if world > 1:
+        t = torch.tensor([ms64], device=dev)
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        ms64 = float(t.item())
+
+    # end to end through the C-ABI with host buffers (pinned)
+    hu = torch.from_numpy(G.random_coefficients(N, N_STATES, prob.seed)).pin_memory()
+    hv = torch.empty_like(hu).pin_memory()
+    hs = torch.empty_like(hu).pin_memory()
+    L = _lib.load()
+    import ctypes as C
+
+    def e2e_once():
+        _lib.check(L.qpgpu_h_s2_u0(wf.ctx, C.c_void_p(hv.data_ptr()), C.c_void_p(hs.data_ptr()),
+                                   C.c_void_p(hu.data_ptr()), N_STATES, N), wf.ctx)
+
+    for _ in range(args.warmup):
+        e2e_once()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        e2e_once()
+    e2e_s = (time.perf_counter() - t0) / args.steps
+
+    # correctness spot check of the e2e result against the device path
+    ref = torch.empty_like(u0)
+    refs = torch.empty_like(u0)
+    wf.h_s2_u0_device(ref, refs, u0, FP64, torch.cuda.current_stream())
+    torch.cuda.synchronize()
+    rel = float((ref.cpu() - hv).abs().max() / ref.abs().max())
+
+    peak, peak_kind = measured_peak_hbm()
+    nint = prob.n_int
+    alg_bytes = N * N_STATES * 8 * 3 + N * (2 * nint * 8 + 12) + P * N_STATES * 8
+    stored_bytes = P * (4 + 8) + N * N_STATES * 8 * 3 + N * 28
+    achieved = alg_bytes / (ms64 * 1e-3) / 1e9
+    traffic, tnote = profiled_traffic(N, P)
+    value = world * N * N_STATES / (ms64 * 1e-3)
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms64, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": workload_config(prob),
+        "setup_s": info["setup_ms"] / 1e3,
+        "n_pairs": P,
+        "sigma_including_setup": N * N_STATES / (info["setup_ms"] * 1e-3 + ms64 * 1e-3),
+        "sigma_fp32": {"value": N * N_STATES / (ms32 * 1e-3), "unit": UNIT, "ms_per_step": ms32,
+                       "dtype": "f32 (Kahan sums, FP64 diagonal)"},
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                     "frac": achieved / peak, "traffic": traffic, "peak_kind": peak_kind,
+                     "kernel": "k_sigma64<4>",
+                     "algorithmic_bytes_per_launch": alg_bytes,
+                     "stored_pair_bytes_per_launch": stored_bytes,
+                     "stored_pair_frac": stored_bytes / (ms64 * 1e-3) / 1e9 / peak,
+                     "note": "algorithmic bytes count one gather of C_J per pair (L2-resident at this size); "
+                             "stored_pair_frac is the HBM fraction of the bytes the kernel must stream"},
+        "e2e": {"value": N * N_STATES / e2e_s, "unit": UNIT, "h2d_bytes_per_step": N * N_STATES * 8,
+                "d2h_bytes_per_step": 2 * N * N_STATES * 8, "max_rel_diff_vs_device": rel},
+        "gpu_launches": launches_per_sigma * args.steps,
+        "clocks": clk.summary(),
+    }
+    if cpu:
+        line["cpu_baseline"] = cpu
+    if traffic is not None:
+        line["roofline"]["traffic_note"] = tnote
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    if world > 1:
+        torch.distributed.destroy_process_group()
+    return 0
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        return run_reference(args)
+    return run_ours(args)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -15,7 +15,9 @@
  *  - Vectors u_0(sze,N_st) are column-major double precision, leading
  *    dimension `ld` >= N_det, determinants in psi_det order.
  *  - "host" arguments are host pointers (the call copies); "device" arguments
- *    are device pointers on the context's GPU.
+ *    are device pointers on the context's GPU.  A NULL `stream` selects the
+ *    context's own stream; pass cudaStreamLegacy ((void*)1) for the legacy
+ *    default stream.
  *  - A context may be used by one host thread at a time (calls lock it).
  */
 #ifndef QPGPU_H
@@ -52,6 +54,7 @@ typedef struct qpgpu_info {
   double setup_ms;        /* device time of the last qpgpu_set_dets */
   double ref_energy;      /* ref_bitmask_energy */
   int64_t device_bytes;   /* device memory held by the context */
+  int64_t n_split_rows;   /* rows whose pairs span several sigma work chunks */
 } qpgpu_info;
 
 /* Context for one orbital space; replaces the IRPF90 providers N_int,

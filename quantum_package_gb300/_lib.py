@@ -30,7 +30,8 @@ class QPGPUError(RuntimeError):
 class Info(C.Structure):
     _fields_ = [("n_det", C.c_int64), ("n_alpha_unique", C.c_int32), ("n_beta_unique", C.c_int32),
                 ("n_pairs", C.c_int64), ("n_s2_pairs", C.c_int64), ("setup_ms", C.c_double),
-                ("ref_energy", C.c_double), ("device_bytes", C.c_int64)]
+                ("ref_energy", C.c_double), ("device_bytes", C.c_int64),
+                ("n_split_rows", C.c_int64)]
 
 
 class DavidsonParams(C.Structure):

@@ -1,5 +1,6 @@
 // C-ABI entry points: context, integral tables, determinant set, sigma.
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 
 #include "qpgpu_internal.cuh"
@@ -146,6 +147,22 @@ int ensure_work(qpgpu_ctx* c, size_t bytes) {
   return 0;
 }
 
+}  // namespace
+
+void qp_report_marks(qpgpu_ctx* c) {
+  if (!c->profile || c->marks.size() < 2) return;
+  cudaEventSynchronize(c->marks.back().second);
+  for (size_t i = 1; i < c->marks.size(); ++i) {
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, c->marks[i - 1].second, c->marks[i].second);
+    fprintf(stderr, "[qpgpu] %-22s %10.3f ms\n", c->marks[i].first.c_str(), ms);
+  }
+  for (auto& m : c->marks) cudaEventDestroy(m.second);
+  c->marks.clear();
+}
+
+namespace {
+
 struct Lock {
   std::mutex& m;
   explicit Lock(std::mutex& mm) : m(mm) { m.lock(); }
@@ -167,6 +184,10 @@ int qpgpu_create(int n_mo, int n_alpha, int n_beta, int n_int, qpgpu_ctx** out) 
   c->na = n_alpha;
   c->nb = n_beta;
   c->nint = n_int;
+  {
+    const char* pe = getenv("QPGPU_PROFILE");
+    c->profile = pe && pe[0] == '1';
+  }
   if (cudaGetDevice(&c->device) != cudaSuccess || cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking) != cudaSuccess) {
     cudaGetLastError();
     delete c;
@@ -186,6 +207,7 @@ int qpgpu_destroy(qpgpu_ctx* c) {
     qp_free_dets(c);
     free_ints(c);
     dev_free(c->d_work);
+    dev_free(c->d_stage);
     cudaStreamDestroy(c->stream);
   }
   delete c;
@@ -211,6 +233,7 @@ int qpgpu_get_info(qpgpu_ctx* c, qpgpu_info* info) {
   if (c->have_pairs) b += P * 16 + c->P_s2 * 8 + N * 28;
   b += (int64_t)c->work_bytes;
   info->device_bytes = b;
+  info->n_split_rows = c->items.n_multi;
   return QPGPU_OK;
 }
 
@@ -303,6 +326,7 @@ int qpgpu_set_dets(qpgpu_ctx* c, const uint64_t* psi_det, int64_t n_det) {
   QP_CUDA(c, dev_alloc(&c->d_dets, (size_t)n_det * 2 * nint));
   QP_CUDA(c, cudaMemcpyAsync(c->d_dets, psi_det, (size_t)n_det * 2 * nint * 8, cudaMemcpyHostToDevice, st));
   QP_CUDA(c, cudaEventRecord(e0, st));
+  qp_mark(c, "start");
   c->N = n_det;
   rc = qp_build_index(c);
   if (rc == 0) {
@@ -310,6 +334,8 @@ int qpgpu_set_dets(qpgpu_ctx* c, const uint64_t* psi_det, int64_t n_det) {
     rc = qp_build_pairs(c);
   }
   if (rc == 0) rc = qp_build_sigma_items(c, &c->items);
+  qp_mark(c, "sigma work items");
+  qp_report_marks(c);
   QP_CUDA(c, cudaEventRecord(e1, st));
   QP_CUDA(c, cudaEventSynchronize(e1));
   float ms = 0.f;
@@ -371,10 +397,18 @@ int qpgpu_h_s2_u0(qpgpu_ctx* c, double* v0, double* s0, const double* u0, int n_
   if (rc) return rc;
   if (!v0 || !s0 || !u0 || n_st < 1 || ld < c->N) return qpgpu_fail(c, QPGPU_ERR_ARG, "bad h_s2_u0 arguments");
   const int64_t N = c->N;
-  double* buf = nullptr;
   const size_t cols = (size_t)N * n_st;
-  QP_CUDA(c, cudaMalloc((void**)&buf, 3 * cols * sizeof(double)));
-  double *du = buf, *dv = buf + cols, *ds = buf + 2 * cols;
+  {
+    Lock l(c->mu);
+    if (c->stage_bytes < 3 * cols * sizeof(double)) {
+      dev_free(c->d_stage);
+      c->d_stage = nullptr;
+      c->stage_bytes = 0;
+      QP_CUDA(c, cudaMalloc((void**)&c->d_stage, 3 * cols * sizeof(double)));
+      c->stage_bytes = 3 * cols * sizeof(double);
+    }
+  }
+  double *du = c->d_stage, *dv = du + cols, *ds = du + 2 * cols;
   cudaStream_t st = c->stream;
   rc = 0;
   if (cudaMemcpy2DAsync(du, N * sizeof(double), u0, ld * sizeof(double), N * sizeof(double), n_st,
@@ -387,7 +421,6 @@ int qpgpu_h_s2_u0(qpgpu_ctx* c, double* v0, double* s0, const double* u0, int n_
                                 cudaMemcpyDeviceToHost, st) != cudaSuccess))
     rc = qpgpu_fail(c, QPGPU_ERR_CUDA, "copy of v_0/s_0 failed");
   cudaError_t e = cudaStreamSynchronize(st);
-  cudaFree(buf);
   if (!rc && e != cudaSuccess) rc = qpgpu_fail(c, QPGPU_ERR_CUDA, cudaGetErrorString(e));
   return rc;
 }

@@ -372,6 +372,7 @@ int qp_build_index(qpgpu_ctx* c) {
   if (rc) return rc;
   rc = unique_spin(c, 1, bid.p, &c->d_beta, &c->Ub);
   if (rc) return rc;
+  qp_mark(c, "unique strings");
   const int Ua = c->Ua, Ub = c->Ub;
   // beta-major bilinear order: key = beta_id * Ua + alpha_id (spindeterminants.irp.f:417)
   QP_CUDA(c, dev_alloc(&c->d_order, N));
@@ -407,12 +408,14 @@ int qp_build_index(qpgpu_ctx* c) {
     k_gather_int<<<grid_for(N), TPB, 0, st>>>(c->d_cols, c->d_t_order, c->d_t_cols, N);
     k_seg_starts<<<grid_for(N), TPB, 0, st>>>(trows.p, c->d_row_loc, N, Ua);
   }
+  qp_mark(c, "bilinear index");
   // singles among unique strings, and the per-string costs of the two
   // alpha-beta scan strategies
   rc = singles_adjacency(c, c->d_alpha, Ua, c->na, &c->d_sa_ptr, &c->d_sa_idx, &c->n_sa);
   if (rc) return rc;
   rc = singles_adjacency(c, c->d_beta, Ub, c->nb, &c->d_sb_ptr, &c->d_sb_idx, &c->n_sb);
   if (rc) return rc;
+  qp_mark(c, "singles adjacency");
   QP_CUDA(c, dev_alloc(&c->d_cost_a, (size_t)Ua));
   QP_CUDA(c, dev_alloc(&c->d_cost_b, (size_t)Ub));
   k_single_costs<<<grid_for(Ua), TPB, 0, st>>>(c->d_sa_ptr, c->d_sa_idx, c->d_row_loc, c->d_cost_a, Ua);

@@ -423,9 +423,13 @@ int build_pairs_t(qpgpu_ctx* c) {
   a.cntS = cS.p;
   const unsigned gAB = nblocks(N, BLK);
   const unsigned gC = nblocks(N * 32, BLK);
+  qp_mark(c, "pair setup");
   k_class_a<NINT, false><<<gAB, BLK, 0, st>>>(a);
+  qp_mark(c, "count A (same beta)");
   k_class_b<NINT, false><<<gAB, BLK, 0, st>>>(a);
+  qp_mark(c, "count B (same alpha)");
   k_class_c<NINT, false><<<gC, BLK, 0, st>>>(a);
+  qp_mark(c, "count C (alpha x beta)");
   QP_CUDA(c, cudaGetLastError());
   Scoped<int64_t> tot, stot;
   QP_CUDA(c, dev_alloc(&tot.p, N + 1));
@@ -461,9 +465,13 @@ int build_pairs_t(qpgpu_ctx* c) {
   QP_CUDA(c, dev_alloc(&err.p, 1));
   QP_CUDA(c, cudaMemsetAsync(err.p, 0, sizeof(int), st));
   a.err = err.p;
+  qp_mark(c, "scan + alloc");
   k_class_a<NINT, true><<<gAB, BLK, 0, st>>>(a);
+  qp_mark(c, "fill A");
   k_class_b<NINT, true><<<gAB, BLK, 0, st>>>(a);
+  qp_mark(c, "fill B");
   k_class_c<NINT, true><<<gC, BLK, 0, st>>>(a);
+  qp_mark(c, "fill C");
   QP_CUDA(c, cudaGetLastError());
   int herr = 0;
   QP_CUDA(c, cudaMemcpyAsync(&herr, err.p, sizeof(int), cudaMemcpyDeviceToHost, st));
@@ -474,6 +482,7 @@ int build_pairs_t(qpgpu_ctx* c) {
   QP_CUDA(c, dev_alloc(&c->d_hdiag32, N));
   k_diag<NINT><<<nblocks(N, 256), 256, 0, st>>>(c->tab, c->d_alpha, c->d_beta, c->d_rows, c->d_cols, c->d_hdiag,
                                                  c->d_sdiag, c->d_hdiag32, N);
+  qp_mark(c, "diagonal");
   QP_CUDA(c, cudaGetLastError());
   QP_CUDA(c, cudaStreamSynchronize(st));
   return 0;

@@ -369,10 +369,15 @@ struct qpgpu_ctx {
   float* d_hdiag32 = nullptr;
   double setup_ms = 0.0;
   SigmaItems items;
+  // optional phase timing of the set-up (environment QPGPU_PROFILE=1)
+  bool profile = false;
+  std::vector<std::pair<std::string, cudaEvent_t>> marks;
 
   // scratch for the host-pointer sigma entry points
   double* d_work = nullptr;
   size_t work_bytes = 0;
+  double* d_stage = nullptr;  // device copies of the host arrays of qpgpu_h_s2_u0
+  size_t stage_bytes = 0;
 };
 
 // error helpers ---------------------------------------------------------------
@@ -405,3 +410,13 @@ void qp_to_bilinear(const double* u0, int64_t ld, const int* order, double* ut, 
 void qp_from_bilinear(const double* vt, int64_t ld, const int* order, double* v0, int nst, int64_t N,
                       cudaStream_t st);
 void qp_to_float(const double* x, float* y, int64_t n, cudaStream_t st);
+
+// records a named event on the context stream when profiling is on
+inline void qp_mark(qpgpu_ctx* c, const char* name) {
+  if (!c->profile) return;
+  cudaEvent_t e;
+  if (cudaEventCreate(&e) != cudaSuccess) return;
+  cudaEventRecord(e, c->stream);
+  c->marks.emplace_back(name, e);
+}
+void qp_report_marks(qpgpu_ctx* c);  // ctx.cu

@@ -25,6 +25,15 @@ def _p(a):
     return C.c_void_p(a.ctypes.data) if a is not None else None
 
 
+def stream_handle(stream):
+    """C-ABI stream argument: NULL selects the context's stream, so torch's
+    legacy default stream (handle 0) is passed as cudaStreamLegacy (0x1)."""
+    if stream is None:
+        return None
+    h = stream.cuda_stream
+    return C.c_void_p(h if h else 1)
+
+
 class Wavefunction:
     """Providers of one orbital space and determinant set, on the GPU."""
 
@@ -101,13 +110,13 @@ class Wavefunction:
     def h_s2_u0_device(self, v0, s0, u0, precision=FP64, stream=None):
         """torch CUDA tensors (N_st, ld) float64; asynchronous on `stream` (torch stream or None)."""
         n_st, ld = u0.shape
-        st = C.c_void_p(stream.cuda_stream) if stream is not None else None
+        st = stream_handle(stream)
         check(_lib.load().qpgpu_h_s2_u0_device(self._ctx, C.c_void_p(v0.data_ptr()), C.c_void_p(s0.data_ptr()),
                                                C.c_void_p(u0.data_ptr()), n_st, ld, precision, st), self._ctx)
 
     def sigma_bilinear(self, v_t, s_t, u_t, u_t32=None, precision=FP64, stream=None):
         """Internal layout: torch CUDA tensors (N_det, N_st), bilinear order."""
-        st = C.c_void_p(stream.cuda_stream) if stream is not None else None
+        st = stream_handle(stream)
         p32 = C.c_void_p(u_t32.data_ptr()) if u_t32 is not None else None
         check(_lib.load().qpgpu_sigma_bilinear(self._ctx, C.c_void_p(v_t.data_ptr()), C.c_void_p(s_t.data_ptr()),
                                                C.c_void_p(u_t.data_ptr()), p32, u_t.shape[1], precision, st),
