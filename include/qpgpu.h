@@ -108,6 +108,21 @@ int qpgpu_h_s2_u0_device(qpgpu_ctx* ctx, double* v0, double* s0, const double* u
 int qpgpu_sigma_bilinear(qpgpu_ctx* ctx, double* v_t, double* s_t, const double* u_t, const float* u_t32,
                          int n_st, int precision, void* stream);
 
+/* No counterpart in the reference.  qpgpu_sigma_bilinear without any device
+ * allocation, for callers that cannot let the library call cudaMalloc (a host
+ * code whose device memory belongs to its own pool allocator, or a worker that
+ * overlaps sigma with work on other streams and cannot afford the device-wide
+ * synchronisation of cudaMalloc/cudaFree).  Same arguments and results.  Its
+ * scratch (partial sums of rows split over several work chunks) is a fixed
+ * 8 MiB device array of the library, held by every GPU that loads it until
+ * exit: the call fails with QPGPU_ERR_ARG when work chunks x n_st exceeds
+ * 524288 (about 100k determinants at 4 states).  The first call on a device
+ * looks up the array's device address (cudaGetSymbolAddress); make that first
+ * call before any stream capture.  All calls share the array: calls that may
+ * overlap on the GPU (other streams, other contexts on the same device) race. */
+int qpgpu_sigma_bilinear_noalloc(qpgpu_ctx* ctx, double* v_t, double* s_t, const double* u_t,
+                                 const float* u_t32, int n_st, int precision, void* stream);
+
 /* psi_bilinear_matrix_order (spindeterminants.irp.f:387-445), 0-based, host:
  * order[k] = psi_det index of bilinear position k. */
 int qpgpu_bilinear_order(qpgpu_ctx* ctx, int32_t* order);

@@ -70,6 +70,7 @@ def load():
         "qpgpu_h_s2_u0_work": (C.c_int, [vp, vp, vp, vp, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int]),
         "qpgpu_h_s2_u0_device": (C.c_int, [vp, vp, vp, vp, C.c_int, C.c_int64, C.c_int, vp]),
         "qpgpu_sigma_bilinear": (C.c_int, [vp, vp, vp, vp, vp, C.c_int, C.c_int, vp]),
+        "qpgpu_sigma_bilinear_noalloc": (C.c_int, [vp, vp, vp, vp, vp, C.c_int, C.c_int, vp]),
         "qpgpu_bilinear_order": (C.c_int, [vp, vp]),
         "qpgpu_diag": (C.c_int, [vp, vp, vp]),
         "qpgpu_connected_pairs": (C.c_int, [vp, C.POINTER(C.c_int64), vp, vp, vp, vp, vp, vp, C.c_int64]),

@@ -365,3 +365,101 @@ void qp_from_bilinear(const double* vt, int64_t ld, const int* order, double* v0
 void qp_to_float(const double* x, float* y, int64_t n, cudaStream_t st) {
   k_to_float<<<gsz(n, 256), 256, 0, st>>>(x, y, n);
 }
+
+// ---------------------------------------------------------------------------
+// Sigma without device allocation.
+//
+// qpgpu_sigma_bilinear keeps its per-chunk partial sums (rows whose pairs span
+// several work chunks) in a buffer that it grows with cudaMalloc on first use.
+// Some callers cannot let a library call cudaMalloc: a host code whose device
+// memory is owned by its own pool allocator (cudaMalloc fails or fragments the
+// pool), or a worker that overlaps sigma with copies and communication on
+// other streams, where cudaMalloc/cudaFree would synchronise the device.  For
+// them the scratch lives in a fixed device array below, of
+// QP_NOALLOC_SLOTS doubles for each of the two sums (8 MiB in total), which
+// every GPU that loads this library holds until the process exits.
+// ---------------------------------------------------------------------------
+#define QP_NOALLOC_SLOTS (1 << 19)
+static __device__ __align__(256) double g_noalloc_partials[2 * QP_NOALLOC_SLOTS];
+
+namespace {
+constexpr int kMaxDevices = 64;
+std::mutex g_noalloc_mu;
+double* g_noalloc_ptr[kMaxDevices] = {nullptr};  // device address of the array, per device
+}  // namespace
+
+extern "C" int qpgpu_sigma_bilinear_noalloc(qpgpu_ctx* c, double* v_t, double* s_t, const double* u_t,
+                                            const float* u_t32, int n_st, int precision, void* stream) {
+  if (!c) return QPGPU_ERR_ARG;
+  if (!c->have_ints || !c->have_pairs) return qpgpu_fail(c, QPGPU_ERR_STATE, "determinants not set");
+  if (!v_t || !s_t || !u_t || n_st < 1 || n_st > 8 || (precision != QPGPU_FP64 && precision != QPGPU_FP32) ||
+      (precision == QPGPU_FP32 && !u_t32))
+    return qpgpu_fail(c, QPGPU_ERR_ARG, "bad sigma arguments (n_st must be 1..8)");
+  std::lock_guard<std::mutex> lk(c->mu);
+  const SigmaItems* it = &c->items;
+  if (it->n_items * (int64_t)n_st > (int64_t)QP_NOALLOC_SLOTS)
+    return qpgpu_fail(c, QPGPU_ERR_ARG,
+                      "no-alloc sigma: work chunks x n_st exceeds the fixed scratch of 524288 slots");
+  // device address of the scratch array on this context's device, looked up
+  // once per device (in host code the array's name is not a device address)
+  if (c->device < 0 || c->device >= kMaxDevices) return qpgpu_fail(c, QPGPU_ERR_ARG, "device ordinal too large");
+  double* scratch = nullptr;
+  {
+    std::lock_guard<std::mutex> g(g_noalloc_mu);
+    if (!g_noalloc_ptr[c->device]) {
+      int cur = -1;
+      if (cudaGetDevice(&cur) != cudaSuccess) return qpgpu_fail(c, QPGPU_ERR_CUDA, "cudaGetDevice failed");
+      if (cur != c->device && cudaSetDevice(c->device) != cudaSuccess)
+        return qpgpu_fail(c, QPGPU_ERR_CUDA, "cudaSetDevice failed");
+      void* p = nullptr;
+      const cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_partials);
+      if (cur != c->device) cudaSetDevice(cur);
+      if (e != cudaSuccess) return qpgpu_fail(c, QPGPU_ERR_CUDA, "cudaGetSymbolAddress of the sigma scratch failed");
+      g_noalloc_ptr[c->device] = (double*)p;
+    }
+    scratch = g_noalloc_ptr[c->device];
+  }
+  SigArgs a{};
+  a.N = c->N;
+  a.rowptr = c->d_rowptr;
+  a.colidx = c->d_colidx;
+  a.val64 = c->d_val64;
+  a.val32 = c->d_val32;
+  a.s2ptr = c->d_s2ptr;
+  a.s2col = c->d_s2col;
+  a.s2val = c->d_s2val;
+  a.hdiag = c->d_hdiag;
+  a.sdiag = c->d_sdiag;
+  a.item_row = it->item_row;
+  a.item_sub = it->item_sub;
+  a.row_nitems = it->row_nitems;
+  a.n_items = it->n_items;
+  a.u = u_t;
+  a.u32 = u_t32;
+  a.v = v_t;
+  a.s = s_t;
+  a.pv = scratch;  // every slot read by k_sigma_combine is written earlier in the same call
+  a.ps = scratch + QP_NOALLOC_SLOTS;
+  a.row_lo = 0;
+  a.row_hi = (int)c->N;
+  a.row_first = 0;
+  a.row_step = 1;
+  cudaStream_t st = stream ? (cudaStream_t)stream : c->stream;
+  const unsigned grid = gsz(it->n_items * 32, SBLK);
+  switch (n_st) {
+    case 1: launch_sigma<1>(a, precision, grid, st); break;
+    case 2: launch_sigma<2>(a, precision, grid, st); break;
+    case 3: launch_sigma<3>(a, precision, grid, st); break;
+    case 4: launch_sigma<4>(a, precision, grid, st); break;
+    case 5: launch_sigma<5>(a, precision, grid, st); break;
+    case 6: launch_sigma<6>(a, precision, grid, st); break;
+    case 7: launch_sigma<7>(a, precision, grid, st); break;
+    default: launch_sigma<8>(a, precision, grid, st); break;
+  }
+  if (it->n_multi > 0)
+    k_sigma_combine<<<gsz((int64_t)it->n_multi * n_st, 256), 256, 0, st>>>(a, it->multi_rows, it->row_item0,
+                                                                          it->n_multi, n_st);
+  const cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return qpgpu_fail(c, QPGPU_ERR_CUDA, cudaGetErrorString(e));
+  return QPGPU_OK;
+}
