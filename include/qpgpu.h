@@ -104,7 +104,8 @@ int qpgpu_h_s2_u0_device(qpgpu_ctx* ctx, double* v0, double* s0, const double* u
 /* Sigma in the internal layout: u_t, v_t, s_t are device arrays (N_det, n_st)
  * with states fastest, determinants in bilinear order (the order of
  * qpgpu_bilinear_order).  u_t32 (FP32 copy of u_t) is required for
- * QPGPU_FP32 and ignored otherwise.  Asynchronous on `stream`. */
+ * QPGPU_FP32 and ignored otherwise; both must be 16-byte aligned.
+ * Asynchronous on `stream`. */
 int qpgpu_sigma_bilinear(qpgpu_ctx* ctx, double* v_t, double* s_t, const double* u_t, const float* u_t32,
                          int n_st, int precision, void* stream);
 
@@ -122,6 +123,45 @@ int qpgpu_sigma_bilinear(qpgpu_ctx* ctx, double* v_t, double* s_t, const double*
  * overlap on the GPU (other streams, other contexts on the same device) race. */
 int qpgpu_sigma_bilinear_noalloc(qpgpu_ctx* ctx, double* v_t, double* s_t, const double* u_t,
                                  const float* u_t32, int n_st, int precision, void* stream);
+
+/* Davidson parameters: the EZFIO knobs of src/Davidson/EZFIO.cfg:1-36 and
+ * src/Determinants/EZFIO.cfg:13-41 plus the precision options. */
+typedef struct qpgpu_davidson_params {
+  int32_t n_states;         /* N_st */
+  int32_t n_states_diag;    /* N_st_diag (<= 8) */
+  int32_t davidson_sze_max; /* micro-iterations before re-contraction (8) */
+  int32_t s2_eig;           /* keep Ritz vectors with |S^2 - expected| < 0.6 (1) */
+  double threshold;         /* threshold_davidson on the squared step norm (1e-12) */
+  int32_t precision;        /* QPGPU_FP64, or QPGPU_FP32: FP32 sigma with an FP64 sigma at each restart */
+  int32_t defect_every;     /* FP32 mode: restart (FP64 sigma) at least every k iterations (0: sze_max) */
+  int32_t preconditioner;   /* 0: the reference's diagonal step */
+  int32_t max_iter;         /* cap on sigma applications (0: 1000) */
+  double energy_tol;        /* reserved */
+} qpgpu_davidson_params;
+
+/* Optional per-iteration record of a Davidson run. */
+typedef struct qpgpu_davidson_trace {
+  int32_t cap;              /* entries available in the arrays below */
+  int32_t n;                /* iterations recorded */
+  int32_t n_sigma;          /* sigma applications */
+  int32_t converged;        /* 1 when the threshold was met */
+  int32_t* sigma_precision; /* [cap] precision of each iteration's sigma */
+  double* energies;         /* [cap][n_states] Ritz values */
+  double* residuals;        /* [cap][n_states] squared step norms */
+  double* elapsed_ms;       /* [cap] device time from the start of the call */
+} qpgpu_davidson_trace;
+
+/* davidson_diag_hs2 / davidson_diag_hjj_sjj
+ * (src/Davidson/diagonalization_hs2.irp.f:1-444) on the context's determinant
+ * set, host arrays: u_in(dim_in, n_states_diag) column-major in psi_det order
+ * holds ALL guess vectors (the reference draws the extra ones with
+ * random_number, :188-200) and returns the eigenvectors; energies and s2_out
+ * get n_states_diag entries (electronic energies, S^2 with the S_z(S_z-1)
+ * shift).  H_jj is diag_H_mat_elem.  Returns the number of sigma
+ * applications (> 0) or a negative status (QPGPU_ERR_DAVIDSON when a residual
+ * exceeds 1e8, as the reference's 'Davidson failed'). */
+int qpgpu_davidson_hs2(qpgpu_ctx* ctx, double* u_in, int64_t dim_in, double* energies, double* s2_out,
+                       const qpgpu_davidson_params* params, qpgpu_davidson_trace* trace);
 
 /* psi_bilinear_matrix_order (spindeterminants.irp.f:387-445), 0-based, host:
  * order[k] = psi_det index of bilinear position k. */

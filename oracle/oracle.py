@@ -209,7 +209,7 @@ class Oracle:
         lib().qpo_dense(self._h, _ptr(H), _ptr(S))
         return H, S
 
-    def davidson(self, guess, n_states, davidson_sze_max=8, threshold=1e-12, s2_eig=True, max_sigma=0):
+    def davidson(self, guess, n_states, davidson_sze_max=8, threshold=1e-12, s2_eig=True, max_sigma=500):
         """guess: (N_st_diag, N).  Returns (energies, s2, vectors, n_sigma, residuals)."""
         u = np.ascontiguousarray(guess, dtype=np.float64).copy()
         nsd, n = u.shape

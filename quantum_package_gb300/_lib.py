@@ -41,6 +41,12 @@ class DavidsonParams(C.Structure):
                 ("energy_tol", C.c_double)]
 
 
+class DavidsonTrace(C.Structure):
+    _fields_ = [("cap", C.c_int32), ("n", C.c_int32), ("n_sigma", C.c_int32), ("converged", C.c_int32),
+                ("sigma_precision", C.c_void_p), ("energies", C.c_void_p), ("residuals", C.c_void_p),
+                ("elapsed_ms", C.c_void_p)]
+
+
 _lib = None
 vp = C.c_void_p
 
@@ -75,9 +81,9 @@ def load():
         "qpgpu_diag": (C.c_int, [vp, vp, vp]),
         "qpgpu_connected_pairs": (C.c_int, [vp, C.POINTER(C.c_int64), vp, vp, vp, vp, vp, vp, C.c_int64]),
     }
-    optional = {
-        "qpgpu_davidson_hs2": (C.c_int, [vp, vp, C.c_int64, vp, vp, C.POINTER(DavidsonParams), vp]),
-    }
+    optional = {}
+    sig["qpgpu_davidson_hs2"] = (C.c_int, [vp, vp, C.c_int64, vp, vp, C.POINTER(DavidsonParams),
+                                           C.POINTER(DavidsonTrace)])
     for name, (res, args) in sig.items():
         f = getattr(L, name)
         f.restype, f.argtypes = res, args

@@ -359,6 +359,8 @@ int qpgpu_sigma_bilinear(qpgpu_ctx* c, double* v_t, double* s_t, const double* u
   if (rc) return rc;
   if (!v_t || !s_t || !u_t || n_st < 1 || n_st > 8 || (precision != QPGPU_FP64 && precision != QPGPU_FP32))
     return qpgpu_fail(c, QPGPU_ERR_ARG, "bad sigma arguments (n_st must be 1..8)");
+  if (((uintptr_t)u_t & 15) || (u_t32 && ((uintptr_t)u_t32 & 15)))
+    return qpgpu_fail(c, QPGPU_ERR_ARG, "u_t and u_t32 must be 16-byte aligned");
   Lock l(c->mu);
   cudaStream_t st = stream ? (cudaStream_t)stream : c->stream;
   return qp_sigma_launch(c, &c->items, v_t, s_t, u_t, u_t32, n_st, precision, st, 0, (int)c->N, 0, 1);

@@ -39,78 +39,150 @@ struct SigArgs {
   int row_step, row_first;
 };
 
-__device__ __forceinline__ double warp_sum(double x) {
-#pragma unroll
-  for (int o = 16; o > 0; o >>= 1) x += __shfl_xor_sync(0xffffffffu, x, o);
-  return x;
-}
-
 __device__ __forceinline__ bool row_selected(const SigArgs& a, int k) {
   if (k < a.row_lo || k >= a.row_hi) return false;
   return ((k - a.row_first) % a.row_step) == 0;
 }
 
+// ---- cross-lane reductions ---------------------------------------------
+// Reduce-scatter of NSTP per-lane partial sums over the 32 lanes of a warp:
+// each round halves the values a lane keeps (exchanging the other half with
+// its partner), then plain butterflies finish.  A lane performs
+// log2(NSTP) + ... = 5 + NSTP - 1 - log2(NSTP) additions instead of 5 * NSTP,
+// which matters on GB300 where FP64 issue is scarce.  On return acc[0] of lane
+// L holds the full sum of state (L >> (5 - log2 NSTP)).  The order of the
+// additions is fixed, so results are deterministic.
+template <int NSTP>
+__device__ __forceinline__ double reduce_scatter64(double (&acc)[NSTP], int lane) {
+  int off = 16;
+#pragma unroll
+  for (int m = NSTP; m > 1; m >>= 1, off >>= 1) {
+    const bool up = lane & off;
+#pragma unroll
+    for (int i = 0; i < m / 2; ++i) {
+      const double send = up ? acc[i] : acc[i + m / 2];
+      const double keep = up ? acc[i + m / 2] : acc[i];
+      acc[i] = keep + __shfl_xor_sync(0xffffffffu, send, off);
+    }
+  }
+  double x = acc[0];
+#pragma unroll
+  for (; off > 0; off >>= 1) x += __shfl_xor_sync(0xffffffffu, x, off);
+  return x;
+}
+
+// error-free sum of two floats (Knuth TwoSum)
+__device__ __forceinline__ void two_sum(float a, float b, float& s, float& e) {
+  s = __fadd_rn(a, b);
+  const float bb = __fsub_rn(s, a);
+  e = __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(b, bb));
+}
+
+// float-float (hi, lo) version of reduce_scatter64, all arithmetic in FP32
+template <int NSTP>
+__device__ __forceinline__ void reduce_scatter_ff(float (&hi)[NSTP], float (&lo)[NSTP], int lane, float& rh,
+                                                  float& rl) {
+  int off = 16;
+#pragma unroll
+  for (int m = NSTP; m > 1; m >>= 1, off >>= 1) {
+    const bool up = lane & off;
+#pragma unroll
+    for (int i = 0; i < m / 2; ++i) {
+      const float sh = up ? hi[i] : hi[i + m / 2], sl = up ? lo[i] : lo[i + m / 2];
+      const float kh = up ? hi[i + m / 2] : hi[i], kl = up ? lo[i + m / 2] : lo[i];
+      const float oh = __shfl_xor_sync(0xffffffffu, sh, off), ol = __shfl_xor_sync(0xffffffffu, sl, off);
+      float s, e;
+      two_sum(kh, oh, s, e);
+      const float l = __fadd_rn(__fadd_rn(kl, ol), e);
+      hi[i] = __fadd_rn(s, l);
+      lo[i] = __fsub_rn(l, __fsub_rn(hi[i], s));
+    }
+  }
+  float h = hi[0], l = lo[0];
+#pragma unroll
+  for (; off > 0; off >>= 1) {
+    const float oh = __shfl_xor_sync(0xffffffffu, h, off), ol = __shfl_xor_sync(0xffffffffu, l, off);
+    float s, e;
+    two_sum(h, oh, s, e);
+    const float t = __fadd_rn(__fadd_rn(l, ol), e);
+    h = __fadd_rn(s, t);
+    l = __fsub_rn(t, __fsub_rn(h, s));
+  }
+  rh = h;
+  rl = l;
+}
+
 template <int NST>
-__global__ void __launch_bounds__(SBLK) k_sigma64(SigArgs a) {
-  const int lane = threadIdx.x & 31;
-  const int64_t warp = ((int64_t)blockIdx.x * SBLK + threadIdx.x) >> 5;
-  const int64_t nwarp = ((int64_t)gridDim.x * SBLK) >> 5;
-  for (int64_t it = warp; it < a.n_items; it += nwarp) {
-    const int k = a.item_row[it];
-    if (!row_selected(a, k)) continue;
-    const int j = a.item_sub[it];
-    const int64_t rb = a.rowptr[k], re = a.rowptr[k + 1];
-    const int64_t beg = rb + (int64_t)j * QP_SIGMA_CHUNK;
-    const int64_t end = min(beg + (int64_t)QP_SIGMA_CHUNK, re);
-    double acc[NST], sacc[NST];
+struct Pow2 {
+  static constexpr int v = NST <= 1 ? 1 : NST <= 2 ? 2 : NST <= 4 ? 4 : 8;
+  static constexpr int lg = NST <= 1 ? 0 : NST <= 2 ? 1 : NST <= 4 ? 2 : 3;
+};
+
+// coefficient row of determinant `col`: vector loads where the layout allows
+template <int NST>
+__device__ __forceinline__ void load_row(const double* u, int64_t col, double (&x)[NST]) {
+  const double* p = u + col * NST;
+  if constexpr (NST % 2 == 0) {
 #pragma unroll
-    for (int st = 0; st < NST; ++st) acc[st] = sacc[st] = 0.0;
-    for (int64_t e = beg + lane; e < end; e += 32) {
-      const int col = __ldg(&a.colidx[e]);
-      const double hv = __ldg(&a.val64[e]);
-      const double* uj = a.u + (int64_t)col * NST;
-#pragma unroll
-      for (int st = 0; st < NST; ++st) acc[st] = fma(hv, __ldg(&uj[st]), acc[st]);
+    for (int i = 0; i < NST; i += 2) {
+      const double2 t = __ldg(reinterpret_cast<const double2*>(p + i));
+      x[i] = t.x;
+      x[i + 1] = t.y;
     }
-    if (j == 0) {
-      const int64_t sb = a.s2ptr[k], se = a.s2ptr[k + 1];
-      for (int64_t e = sb + lane; e < se; e += 32) {
-        const int col = __ldg(&a.s2col[e]);
-        const double sv = (double)__ldg(&a.s2val[e]);
-        const double* uj = a.u + (int64_t)col * NST;
+  } else {
 #pragma unroll
-        for (int st = 0; st < NST; ++st) sacc[st] = fma(sv, __ldg(&uj[st]), sacc[st]);
-      }
-    }
-#pragma unroll
-    for (int st = 0; st < NST; ++st) {
-      acc[st] = warp_sum(acc[st]);
-      sacc[st] = warp_sum(sacc[st]);
-    }
-    if (a.row_nitems[k] == 1) {
-      if (lane < NST) {
-        double av = 0.0, as = 0.0, uk = a.u[(int64_t)k * NST + lane];
-#pragma unroll
-        for (int st = 0; st < NST; ++st)
-          if (st == lane) { av = acc[st]; as = sacc[st]; }
-        a.v[(int64_t)k * NST + lane] = av + a.hdiag[k] * uk;
-        a.s[(int64_t)k * NST + lane] = as + a.sdiag[k] * uk;
-      }
-    } else if (lane < NST) {
-      double av = 0.0, as = 0.0;
-#pragma unroll
-      for (int st = 0; st < NST; ++st)
-        if (st == lane) { av = acc[st]; as = sacc[st]; }
-      a.pv[it * NST + lane] = av;
-      a.ps[it * NST + lane] = as;
-    }
+    for (int i = 0; i < NST; ++i) x[i] = __ldg(p + i);
   }
 }
 
-// FP32 matrix elements x FP32 coefficients, Kahan-compensated per lane; lane
-// partials are combined in FP64 and the FP64 diagonal term is added.
 template <int NST>
-__global__ void __launch_bounds__(SBLK) k_sigma32(SigArgs a) {
+__device__ __forceinline__ void load_row(const float* u, int64_t col, float (&x)[NST]) {
+  const float* p = u + col * NST;
+  if constexpr (NST % 4 == 0) {
+#pragma unroll
+    for (int i = 0; i < NST; i += 4) {
+      const float4 t = __ldg(reinterpret_cast<const float4*>(p + i));
+      x[i] = t.x;
+      x[i + 1] = t.y;
+      x[i + 2] = t.z;
+      x[i + 3] = t.w;
+    }
+  } else if constexpr (NST % 2 == 0) {
+#pragma unroll
+    for (int i = 0; i < NST; i += 2) {
+      const float2 t = __ldg(reinterpret_cast<const float2*>(p + i));
+      x[i] = t.x;
+      x[i + 1] = t.y;
+    }
+  } else {
+#pragma unroll
+    for (int i = 0; i < NST; ++i) x[i] = __ldg(p + i);
+  }
+}
+
+// write the reduced state sums (lane L holds state L >> shift) and the diagonal
+template <int NST>
+__device__ __forceinline__ void store_row(const SigArgs& a, int64_t it, int k, int lane, double hv, double sv,
+                                          bool has_s2) {
+  constexpr int SH = 5 - Pow2<NST>::lg;
+  const int st = lane >> SH;
+  const bool owner = (lane & ((1 << SH) - 1)) == 0 && st < NST;
+  if (!owner) return;
+  if (a.row_nitems[k] == 1) {
+    const double uk = a.u[(int64_t)k * NST + st];
+    a.v[(int64_t)k * NST + st] = hv + a.hdiag[k] * uk;
+    a.s[(int64_t)k * NST + st] = (has_s2 ? sv : 0.0) + a.sdiag[k] * uk;
+  } else {
+    a.pv[it * NST + st] = hv;
+    a.ps[it * NST + st] = has_s2 ? sv : 0.0;
+  }
+}
+
+constexpr int UNR = 2;  // pairs per lane per loop trip (independent loads in flight)
+
+template <int NST>
+__global__ void __launch_bounds__(SBLK) k_sigma64(SigArgs a) {
+  constexpr int NP = Pow2<NST>::v;
   const int lane = threadIdx.x & 31;
   const int64_t warp = ((int64_t)blockIdx.x * SBLK + threadIdx.x) >> 5;
   const int64_t nwarp = ((int64_t)gridDim.x * SBLK) >> 5;
@@ -121,59 +193,118 @@ __global__ void __launch_bounds__(SBLK) k_sigma32(SigArgs a) {
     const int64_t rb = a.rowptr[k], re = a.rowptr[k + 1];
     const int64_t beg = rb + (int64_t)j * QP_SIGMA_CHUNK;
     const int64_t end = min(beg + (int64_t)QP_SIGMA_CHUNK, re);
-    float sum[NST], cmp[NST];
-    double acc[NST], sacc[NST];
+    double acc[NP];
 #pragma unroll
-    for (int st = 0; st < NST; ++st) sum[st] = cmp[st] = 0.f;
-    for (int64_t e = beg + lane; e < end; e += 32) {
-      const int col = __ldg(&a.colidx[e]);
-      const float hv = __ldg(&a.val32[e]);
-      const float* uj = a.u32 + (int64_t)col * NST;
+    for (int st = 0; st < NP; ++st) acc[st] = 0.0;
+    for (int64_t e0 = beg + lane; e0 < end; e0 += 32 * UNR) {
+      int col[UNR];
+      double hv[UNR];
 #pragma unroll
-      for (int st = 0; st < NST; ++st) {
-        const float y = __fmaf_rn(hv, __ldg(&uj[st]), -cmp[st]);
-        const float t = __fadd_rn(sum[st], y);
-        cmp[st] = __fsub_rn(__fsub_rn(t, sum[st]), y);
-        sum[st] = t;
+      for (int q = 0; q < UNR; ++q) {
+        const int64_t e = e0 + 32 * q;
+        col[q] = e < end ? __ldg(&a.colidx[e]) : k;
+        hv[q] = e < end ? __ldg(&a.val64[e]) : 0.0;
+      }
+#pragma unroll
+      for (int q = 0; q < UNR; ++q) {
+        double x[NST];
+        load_row<NST>(a.u, col[q], x);
+#pragma unroll
+        for (int st = 0; st < NST; ++st) acc[st] = fma(hv[q], x[st], acc[st]);
       }
     }
+    const double hsum = reduce_scatter64<NP>(acc, lane);
+    double ssum = 0.0;
+    const int64_t sb = a.s2ptr[k], se = a.s2ptr[k + 1];
+    const bool has_s2 = (j == 0) && (se > sb);
+    if (has_s2) {
+      double sacc[NP];
 #pragma unroll
-    for (int st = 0; st < NST; ++st) {
-      acc[st] = (double)sum[st] - (double)cmp[st];
-      sacc[st] = 0.0;
-    }
-    if (j == 0) {
-      const int64_t sb = a.s2ptr[k], se = a.s2ptr[k + 1];
+      for (int st = 0; st < NP; ++st) sacc[st] = 0.0;
       for (int64_t e = sb + lane; e < se; e += 32) {
-        const int col = __ldg(&a.s2col[e]);
         const double sv = (double)__ldg(&a.s2val[e]);
-        const float* uj = a.u32 + (int64_t)col * NST;
+        double x[NST];
+        load_row<NST>(a.u, __ldg(&a.s2col[e]), x);
 #pragma unroll
-        for (int st = 0; st < NST; ++st) sacc[st] = fma(sv, (double)__ldg(&uj[st]), sacc[st]);
+        for (int st = 0; st < NST; ++st) sacc[st] = fma(sv, x[st], sacc[st]);
+      }
+      ssum = reduce_scatter64<NP>(sacc, lane);
+    }
+    store_row<NST>(a, it, k, lane, hsum, ssum, has_s2);
+  }
+}
+
+// FP32 matrix elements x FP32 coefficients with Kahan-compensated lane sums;
+// lanes are combined as float-float pairs, and only the owner lane of each
+// state converts to FP64 and adds the FP64 diagonal term.
+template <int NST>
+__global__ void __launch_bounds__(SBLK) k_sigma32(SigArgs a) {
+  constexpr int NP = Pow2<NST>::v;
+  const int lane = threadIdx.x & 31;
+  const int64_t warp = ((int64_t)blockIdx.x * SBLK + threadIdx.x) >> 5;
+  const int64_t nwarp = ((int64_t)gridDim.x * SBLK) >> 5;
+  for (int64_t it = warp; it < a.n_items; it += nwarp) {
+    const int k = a.item_row[it];
+    if (!row_selected(a, k)) continue;
+    const int j = a.item_sub[it];
+    const int64_t rb = a.rowptr[k], re = a.rowptr[k + 1];
+    const int64_t beg = rb + (int64_t)j * QP_SIGMA_CHUNK;
+    const int64_t end = min(beg + (int64_t)QP_SIGMA_CHUNK, re);
+    float sum[NP], cmp[NP];
+#pragma unroll
+    for (int st = 0; st < NP; ++st) sum[st] = cmp[st] = 0.f;
+    for (int64_t e0 = beg + lane; e0 < end; e0 += 32 * UNR) {
+      int col[UNR];
+      float hv[UNR];
+#pragma unroll
+      for (int q = 0; q < UNR; ++q) {
+        const int64_t e = e0 + 32 * q;
+        col[q] = e < end ? __ldg(&a.colidx[e]) : k;
+        hv[q] = e < end ? __ldg(&a.val32[e]) : 0.f;
+      }
+#pragma unroll
+      for (int q = 0; q < UNR; ++q) {
+        float x[NST];
+        load_row<NST>(a.u32, col[q], x);
+#pragma unroll
+        for (int st = 0; st < NST; ++st) {
+          const float y = __fmaf_rn(hv[q], x[st], -cmp[st]);
+          const float t = __fadd_rn(sum[st], y);
+          cmp[st] = __fsub_rn(__fsub_rn(t, sum[st]), y);
+          sum[st] = t;
+        }
       }
     }
+    // Kahan state (sum, -cmp) is a float-float value
 #pragma unroll
-    for (int st = 0; st < NST; ++st) {
-      acc[st] = warp_sum(acc[st]);
-      sacc[st] = warp_sum(sacc[st]);
-    }
-    if (a.row_nitems[k] == 1) {
-      if (lane < NST) {
-        double av = 0.0, as = 0.0, uk = a.u[(int64_t)k * NST + lane];
+    for (int st = 0; st < NP; ++st) cmp[st] = -cmp[st];
+    float rh, rl;
+    reduce_scatter_ff<NP>(sum, cmp, lane, rh, rl);
+    const double hsum = (double)rh + (double)rl;
+    double ssum = 0.0;
+    const int64_t sb = a.s2ptr[k], se = a.s2ptr[k + 1];
+    const bool has_s2 = (j == 0) && (se > sb);
+    if (has_s2) {
+      float sh[NP], sl[NP];
 #pragma unroll
-        for (int st = 0; st < NST; ++st)
-          if (st == lane) { av = acc[st]; as = sacc[st]; }
-        a.v[(int64_t)k * NST + lane] = av + a.hdiag[k] * uk;
-        a.s[(int64_t)k * NST + lane] = as + a.sdiag[k] * uk;
+      for (int st = 0; st < NP; ++st) sh[st] = sl[st] = 0.f;
+      for (int64_t e = sb + lane; e < se; e += 32) {
+        const float sv = __ldg(&a.s2val[e]);  // +-1: products are exact
+        float x[NST];
+        load_row<NST>(a.u32, __ldg(&a.s2col[e]), x);
+#pragma unroll
+        for (int st = 0; st < NST; ++st) {
+          float s, err;
+          two_sum(sh[st], sv * x[st], s, err);
+          sh[st] = s;
+          sl[st] = __fadd_rn(sl[st], err);
+        }
       }
-    } else if (lane < NST) {
-      double av = 0.0, as = 0.0;
-#pragma unroll
-      for (int st = 0; st < NST; ++st)
-        if (st == lane) { av = acc[st]; as = sacc[st]; }
-      a.pv[it * NST + lane] = av;
-      a.ps[it * NST + lane] = as;
+      float qh, ql;
+      reduce_scatter_ff<NP>(sh, sl, lane, qh, ql);
+      ssum = (double)qh + (double)ql;
     }
+    store_row<NST>(a, it, k, lane, hsum, ssum, has_s2);
   }
 }
 
@@ -395,6 +526,8 @@ extern "C" int qpgpu_sigma_bilinear_noalloc(qpgpu_ctx* c, double* v_t, double* s
   if (!v_t || !s_t || !u_t || n_st < 1 || n_st > 8 || (precision != QPGPU_FP64 && precision != QPGPU_FP32) ||
       (precision == QPGPU_FP32 && !u_t32))
     return qpgpu_fail(c, QPGPU_ERR_ARG, "bad sigma arguments (n_st must be 1..8)");
+  if (((uintptr_t)u_t & 15) || (u_t32 && ((uintptr_t)u_t32 & 15)))
+    return qpgpu_fail(c, QPGPU_ERR_ARG, "u_t and u_t32 must be 16-byte aligned");
   std::lock_guard<std::mutex> lk(c->mu);
   const SigmaItems* it = &c->items;
   if (it->n_items * (int64_t)n_st > (int64_t)QP_NOALLOC_SLOTS)

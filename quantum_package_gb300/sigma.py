@@ -150,3 +150,33 @@ class Wavefunction:
               self._ctx)
         o = np.lexsort((J, I))
         return dict(I=I[o], J=J[o], cls=cls[o], phase=ph[o], exc=exc[o], hij=hij[o])
+
+    # --- Davidson ------------------------------------------------------
+    def davidson_diag_hs2(self, u_in, n_states, davidson_sze_max=8, threshold=1e-12, s2_eig=True,
+                          precision=FP64, defect_every=0, preconditioner=0, max_iter=500, trace_cap=512):
+        """davidson_diag_hs2 (diagonalization_hs2.irp.f:1-49) on this determinant set.
+
+        u_in: (N_st_diag, N) guess vectors (all of them, seeded by the caller).
+        Returns dict(energies, s2, vectors, n_sigma, trace) with electronic energies.
+        """
+        u = np.ascontiguousarray(np.atleast_2d(u_in), dtype=np.float64).copy()
+        nsd, n = u.shape
+        prm = _lib.DavidsonParams(n_states=n_states, n_states_diag=nsd, davidson_sze_max=davidson_sze_max,
+                                  s2_eig=int(bool(s2_eig)), threshold=threshold, precision=precision,
+                                  defect_every=defect_every, preconditioner=preconditioner, max_iter=max_iter,
+                                  energy_tol=0.0)
+        prec = np.zeros(trace_cap, np.int32)
+        en = np.zeros((trace_cap, n_states))
+        rs = np.zeros((trace_cap, n_states))
+        el = np.zeros(trace_cap)
+        tr = _lib.DavidsonTrace(cap=trace_cap, n=0, n_sigma=0, converged=0, sigma_precision=prec.ctypes.data,
+                                energies=en.ctypes.data, residuals=rs.ctypes.data, elapsed_ms=el.ctypes.data)
+        e = np.zeros(nsd)
+        s2 = np.zeros(nsd)
+        rc = _lib.load().qpgpu_davidson_hs2(self._ctx, _p(u), n, _p(e), _p(s2), C.byref(prm), C.byref(tr))
+        if rc < 0:
+            check(rc, self._ctx)
+        k = tr.n
+        return dict(energies=e, s2=s2, vectors=u, n_sigma=rc, converged=bool(tr.converged),
+                    trace=dict(precision=prec[:k].copy(), energies=en[:k].copy(), residuals=rs[:k].copy(),
+                               elapsed_ms=el[:k].copy()))
