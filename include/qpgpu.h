@@ -134,9 +134,10 @@ typedef struct qpgpu_davidson_params {
   double threshold;         /* threshold_davidson on the squared step norm (1e-12) */
   int32_t precision;        /* QPGPU_FP64, or QPGPU_FP32: FP32 sigma with an FP64 sigma at each restart */
   int32_t defect_every;     /* FP32 mode: restart (FP64 sigma) at least every k iterations (0: sze_max) */
-  int32_t preconditioner;   /* 0: the reference's diagonal step */
+  int32_t preconditioner;   /* 0: the reference's diagonal step; 1: learned (MLP) step with fallback */
   int32_t max_iter;         /* cap on sigma applications (0: 1000) */
-  double energy_tol;        /* reserved */
+  int32_t collect_every;    /* > 0: capture training pairs every k iterations (from the 2nd) */
+  int32_t collect_max;      /* captures kept (default 8) */
 } qpgpu_davidson_params;
 
 /* Optional per-iteration record of a Davidson run. */
@@ -149,6 +150,9 @@ typedef struct qpgpu_davidson_trace {
   double* energies;         /* [cap][n_states] Ritz values */
   double* residuals;        /* [cap][n_states] squared step norms */
   double* elapsed_ms;       /* [cap] device time from the start of the call */
+  int32_t n_fallback;       /* states switched back to the diagonal step */
+  int32_t pad;
+  int64_t n_samples;        /* training samples added by this run */
 } qpgpu_davidson_trace;
 
 /* davidson_diag_hs2 / davidson_diag_hjj_sjj
@@ -162,6 +166,27 @@ typedef struct qpgpu_davidson_trace {
  * exceeds 1e8, as the reference's 'Davidson failed'). */
 int qpgpu_davidson_hs2(qpgpu_ctx* ctx, double* u_in, int64_t dim_in, double* energies, double* s2_out,
                        const qpgpu_davidson_params* params, qpgpu_davidson_trace* trace);
+
+/* Learned Davidson preconditioner (no counterpart in the reference): an MLP
+ * 8 -> 64 -> 64 -> 1 (GELU, FP32, 4801 parameters packed W1[64][8], b1[64],
+ * W2[64][64], b2[64], W3[64], b3) that scales the diagonal correction of the
+ * Davidson step per determinant.  Features (8 floats): alpha and beta
+ * excitation rank / 4, (H_II - E)/10, hole/particle orbital-energy sum / 10,
+ * open shells / 8, log10|c_I|/8, log10|r_I|/8, log10|d_I|/8.  Samples are
+ * (features, target multiplier g, weight w); the loss is mean(w (y - g)^2).
+ * The training set and the parameters belong to the context and survive
+ * qpgpu_set_dets (earlier determinant sets train later ones). */
+#define QPGPU_MLP_NPARAM 4801
+int qpgpu_mlp_init(qpgpu_ctx* ctx, uint64_t seed);
+int qpgpu_mlp_set_weights(qpgpu_ctx* ctx, const float* w);
+int qpgpu_mlp_get_weights(qpgpu_ctx* ctx, float* w);
+int qpgpu_mlp_add_samples(qpgpu_ctx* ctx, const float* X, const float* g, const float* w, int64_t n);
+int qpgpu_mlp_clear_samples(qpgpu_ctx* ctx);
+int64_t qpgpu_mlp_n_samples(qpgpu_ctx* ctx);
+int qpgpu_mlp_gradient(qpgpu_ctx* ctx, const float* X, const float* g, const float* w, int64_t n, float* grad,
+                       float* loss);
+int qpgpu_mlp_predict(qpgpu_ctx* ctx, const float* X, int64_t n, float* y);
+int qpgpu_mlp_train(qpgpu_ctx* ctx, int epochs, int batch, float lr, uint64_t seed, float* loss);
 
 /* psi_bilinear_matrix_order (spindeterminants.irp.f:387-445), 0-based, host:
  * order[k] = psi_det index of bilinear position k. */

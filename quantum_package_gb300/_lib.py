@@ -38,13 +38,17 @@ class DavidsonParams(C.Structure):
     _fields_ = [("n_states", C.c_int32), ("n_states_diag", C.c_int32), ("davidson_sze_max", C.c_int32),
                 ("s2_eig", C.c_int32), ("threshold", C.c_double), ("precision", C.c_int32),
                 ("defect_every", C.c_int32), ("preconditioner", C.c_int32), ("max_iter", C.c_int32),
-                ("energy_tol", C.c_double)]
+                ("collect_every", C.c_int32), ("collect_max", C.c_int32)]
 
 
 class DavidsonTrace(C.Structure):
     _fields_ = [("cap", C.c_int32), ("n", C.c_int32), ("n_sigma", C.c_int32), ("converged", C.c_int32),
                 ("sigma_precision", C.c_void_p), ("energies", C.c_void_p), ("residuals", C.c_void_p),
-                ("elapsed_ms", C.c_void_p)]
+                ("elapsed_ms", C.c_void_p), ("n_fallback", C.c_int32), ("pad", C.c_int32),
+                ("n_samples", C.c_int64)]
+
+
+MLP_NPARAM = 4801
 
 
 _lib = None
@@ -78,6 +82,15 @@ def load():
         "qpgpu_sigma_bilinear": (C.c_int, [vp, vp, vp, vp, vp, C.c_int, C.c_int, vp]),
         "qpgpu_sigma_bilinear_noalloc": (C.c_int, [vp, vp, vp, vp, vp, C.c_int, C.c_int, vp]),
         "qpgpu_bilinear_order": (C.c_int, [vp, vp]),
+        "qpgpu_mlp_init": (C.c_int, [vp, C.c_uint64]),
+        "qpgpu_mlp_set_weights": (C.c_int, [vp, vp]),
+        "qpgpu_mlp_get_weights": (C.c_int, [vp, vp]),
+        "qpgpu_mlp_add_samples": (C.c_int, [vp, vp, vp, vp, C.c_int64]),
+        "qpgpu_mlp_clear_samples": (C.c_int, [vp]),
+        "qpgpu_mlp_n_samples": (C.c_int64, [vp]),
+        "qpgpu_mlp_gradient": (C.c_int, [vp, vp, vp, vp, C.c_int64, vp, C.POINTER(C.c_float)]),
+        "qpgpu_mlp_predict": (C.c_int, [vp, vp, C.c_int64, vp]),
+        "qpgpu_mlp_train": (C.c_int, [vp, C.c_int, C.c_int, C.c_float, C.c_uint64, C.POINTER(C.c_float)]),
         "qpgpu_diag": (C.c_int, [vp, vp, vp]),
         "qpgpu_connected_pairs": (C.c_int, [vp, C.POINTER(C.c_int64), vp, vp, vp, vp, vp, vp, C.c_int64]),
     }

@@ -206,6 +206,7 @@ int qpgpu_destroy(qpgpu_ctx* c) {
     qp_free_pairs(c);
     qp_free_dets(c);
     free_ints(c);
+    c->mlp.free_all();
     dev_free(c->d_work);
     dev_free(c->d_stage);
     cudaStreamDestroy(c->stream);
@@ -334,6 +335,7 @@ int qpgpu_set_dets(qpgpu_ctx* c, const uint64_t* psi_det, int64_t n_det) {
     rc = qp_build_pairs(c);
   }
   if (rc == 0) rc = qp_build_sigma_items(c, &c->items);
+  if (rc == 0) rc = qp_det_features(c);
   qp_mark(c, "sigma work items");
   qp_report_marks(c);
   QP_CUDA(c, cudaEventRecord(e1, st));

@@ -41,19 +41,31 @@ inline unsigned gsz(int64_t n, int tpb = DBLK) {
 }
 
 // G[i][j] = sum_r A_i[r] B_j[r] for the m columns of A (stacked blocks of nsd
-// columns, block stride N*nsd) and the nsd columns of B.  One partial per CTA.
+// columns, block stride N*nsd) and the nsd columns of B.  Rows are staged in
+// shared memory; thread t owns column i = t % m of A for every j (register
+// tile of nsd accumulators) over the rows r = t / m (mod 256 / m) of the tile,
+// and the row groups are added in a fixed order.  One partial per CTA.
+// A non-null `skip` flag that is set makes the kernel write zeros (used for
+// the conditional second Gram-Schmidt pass).
 constexpr int GTR = 32;
 __global__ void __launch_bounds__(DBLK) k_gram(const double* A, int m, const double* B, int nsd, int64_t N,
-                                               int64_t rows_per_cta, double* partial) {
+                                               int64_t rows_per_cta, double* partial, const int* skip) {
   extern __shared__ double sm[];
   double* As = sm;                 // [GTR][m]
   double* Bs = sm + GTR * m;       // [GTR][nsd]
+  const int np = m * nsd;
+  if (skip && *skip) {
+    for (int p = threadIdx.x; p < np; p += DBLK) partial[(int64_t)blockIdx.x * np + p] = 0.0;
+    return;
+  }
   const int64_t r0 = (int64_t)blockIdx.x * rows_per_cta;
   const int64_t r1 = min(r0 + rows_per_cta, N);
-  const int np = m * nsd;
-  double acc[MAXM * MAXS / DBLK];
+  const int groups = DBLK / m;  // m <= 128 -> at least 2 groups
+  const int i = threadIdx.x % m, g = threadIdx.x / m;
+  const bool active = g < groups;
+  double acc[MAXS];
 #pragma unroll
-  for (int q = 0; q < MAXM * MAXS / DBLK; ++q) acc[q] = 0.0;
+  for (int j = 0; j < MAXS; ++j) acc[j] = 0.0;
   for (int64_t t0 = r0; t0 < r1; t0 += GTR) {
     const int tr = (int)min((int64_t)GTR, r1 - t0);
     __syncthreads();
@@ -64,21 +76,26 @@ __global__ void __launch_bounds__(DBLK) k_gram(const double* A, int m, const dou
     }
     for (int idx = threadIdx.x; idx < tr * nsd; idx += DBLK) Bs[idx] = B[t0 * nsd + idx];
     __syncthreads();
+    if (active) {
+      for (int r = g; r < tr; r += groups) {
+        const double a = As[r * m + i];
+        const double* brow = &Bs[r * nsd];
 #pragma unroll
-    for (int q = 0; q < MAXM * MAXS / DBLK; ++q) {
-      const int p = threadIdx.x + q * DBLK;
-      if (p < np) {
-        const int i = p / nsd, j = p % nsd;
-        double s = acc[q];
-        for (int r = 0; r < tr; ++r) s = fma(As[r * m + i], Bs[r * nsd + j], s);
-        acc[q] = s;
+        for (int j = 0; j < MAXS; ++j)
+          if (j < nsd) acc[j] = fma(a, brow[j], acc[j]);
       }
     }
   }
-#pragma unroll
-  for (int q = 0; q < MAXM * MAXS / DBLK; ++q) {
-    const int p = threadIdx.x + q * DBLK;
-    if (p < np) partial[(int64_t)blockIdx.x * np + p] = acc[q];
+  __syncthreads();
+  // fixed-order sum over row groups through shared memory (reuses As)
+  double* red = sm;  // [groups][m][nsd]
+  if (active)
+    for (int j = 0; j < nsd; ++j) red[((size_t)g * m + i) * nsd + j] = acc[j];
+  __syncthreads();
+  for (int p = threadIdx.x; p < np; p += DBLK) {
+    double s = 0.0;
+    for (int q = 0; q < groups; ++q) s += red[(size_t)q * np + p];
+    partial[(int64_t)blockIdx.x * np + p] = s;
   }
 }
 
@@ -99,7 +116,9 @@ struct LinComb {
   double* out[3];
   int n;
 };
-__global__ void __launch_bounds__(DBLK) k_lincomb(LinComb L, int m, int nsd, int64_t N, const double* C, int sub) {
+__global__ void __launch_bounds__(DBLK) k_lincomb(LinComb L, int m, int nsd, int64_t N, const double* C, int sub,
+                                                  const int* skip) {
+  if (skip && *skip) return;
   __shared__ double Cs[MAXM * MAXS];
   for (int i = threadIdx.x; i < m * nsd; i += DBLK) Cs[i] = C[i];
   __syncthreads();
@@ -163,6 +182,18 @@ __global__ void k_chol_inv(const double* G, int nsd, double* Rinv) {
     for (int j = 0; j < nsd; ++j) Rinv[i * nsd + j] = Ri[i][j];
 }
 
+// second Gram-Schmidt pass needed?  Yes when a column lost more than half of
+// its norm in the first pass (G0 before, G1 after; diagonals).
+__global__ void k_need_second_pass(const double* G0, const double* G1, int nsd, int* skip) {
+  if (threadIdx.x || blockIdx.x) return;
+  int need = 0;
+  for (int j = 0; j < nsd; ++j) {
+    const double a = G0[j * nsd + j], b = G1[j * nsd + j];
+    if (!(b > 0.25 * a)) need = 1;
+  }
+  *skip = need ? 0 : 1;
+}
+
 struct StepParams {
   double lambda[MAXS];
   double s2[MAXS];
@@ -202,6 +233,143 @@ __global__ void __launch_bounds__(DBLK) k_step(double* Un, const double* Wn, con
     double s = 0.0;
     for (int i = 0; i < DBLK / 32; ++i) s += red[threadIdx.x][i];
     partial[(int64_t)blockIdx.x * MAXS + threadIdx.x] = s;
+  }
+}
+
+// Davidson step with the learned preconditioner: the reference's diagonal
+// correction d (whose squared norm stays the convergence measure) is scaled
+// per determinant by the MLP's multiplier g for the states flagged in
+// p.mlp_mask; other states take d unchanged.
+__global__ void __launch_bounds__(DBLK) k_step_mlp(double* Un, const double* Wn, const double* Sn, const double* hjj,
+                                                   const float4* feat, const float* P, int64_t N, StepParams p,
+                                                   unsigned mlp_mask, double* partial) {
+  __shared__ float Ps[QP_MLP_NPARAM];
+  __shared__ double red[MAXS][DBLK / 32];
+  for (int i = threadIdx.x; i < QP_MLP_NPARAM; i += DBLK) Ps[i] = P[i];
+  __syncthreads();
+  double acc[MAXS];
+#pragma unroll
+  for (int k = 0; k < MAXS; ++k) acc[k] = 0.0;
+  for (int64_t r = blockIdx.x * (int64_t)DBLK + threadIdx.x; r < N; r += (int64_t)gridDim.x * DBLK) {
+    const double h = hjj[r];
+    const float4 st = feat[r];
+    for (int k = 0; k < p.nsd; ++k) {
+      const int64_t x = r * p.nsd + k;
+      const double u = Un[x];
+      const double res = p.lambda[k] * u - Wn[x];
+      const double d = res * (1.0 + p.s2[k] * u - Sn[x] - p.sz2sz) / fmax(h - p.lambda[k], 1e-2);
+      double v = d;
+      if ((mlp_mask >> k) & 1u) {
+        float f[QP_MLP_IN];
+        qp_features(st, h - p.lambda[k], u, res, d, f);
+        v = d * (double)qp_mlp_forward(Ps, f);
+      }
+      Un[x] = v;
+      if (k < p.nst) acc[k] = fma(d, d, acc[k]);
+    }
+  }
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+#pragma unroll
+  for (int k = 0; k < MAXS; ++k) {
+    double s = acc[k];
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+    if (lane == 0) red[k][w] = s;
+  }
+  __syncthreads();
+  if (threadIdx.x < MAXS) {
+    double s = 0.0;
+    for (int i = 0; i < DBLK / 32; ++i) s += red[threadIdx.x][i];
+    partial[(int64_t)blockIdx.x * MAXS + threadIdx.x] = s;
+  }
+}
+
+// training capture: features, diagonal correction d and Ritz vector c of the
+// states k < nst, before the step overwrites the Ritz block
+__global__ void k_capture(const double* Un, const double* Wn, const double* Sn, const double* hjj, const float4* feat,
+                          int64_t N, StepParams p, int slot0, float* cX, float* cd, float* cc) {
+  for (int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; r < N; r += (int64_t)gridDim.x * blockDim.x) {
+    const double h = hjj[r];
+    const float4 st = feat[r];
+    for (int k = 0; k < p.nst; ++k) {
+      const int64_t x = r * p.nsd + k;
+      const double u = Un[x];
+      const double res = p.lambda[k] * u - Wn[x];
+      const double d = res * (1.0 + p.s2[k] * u - Sn[x] - p.sz2sz) / fmax(h - p.lambda[k], 1e-2);
+      const int64_t slot = slot0 + k;
+      float f[QP_MLP_IN];
+      qp_features(st, h - p.lambda[k], u, res, d, f);
+      for (int i = 0; i < QP_MLP_IN; ++i) cX[(slot * N + r) * QP_MLP_IN + i] = f[i];
+      cd[slot * N + r] = (float)d;
+      cc[slot * N + r] = (float)u;
+    }
+  }
+}
+
+// per-CTA sums over rows for each captured slot (state k = slot % nst of the
+// final vectors cf, block 0): mode 0: (cf.c, d.d); mode 1 with dot: (e.e, e.d),
+// e = cf - dot c
+__global__ void k_capture_sums(const double* cf, int nsd, int nst, const float* cd, const float* cc, int nslot,
+                               int64_t N, const double* dot, int mode, double* partial) {
+  __shared__ double red[2][DBLK];
+  for (int s = 0; s < nslot; ++s) {
+    const int k = s % nst;
+    double a = 0.0, b = 0.0;
+    for (int64_t r = blockIdx.x * (int64_t)DBLK + threadIdx.x; r < N; r += (int64_t)gridDim.x * DBLK) {
+      const double c = cc[(int64_t)s * N + r], d = cd[(int64_t)s * N + r], f = cf[r * nsd + k];
+      if (mode == 0) {
+        a = fma(f, c, a);
+        b = fma(d, d, b);
+      } else {
+        const double e = f - dot[s] * c;
+        a = fma(e, e, a);
+        b = fma(e, d, b);
+      }
+    }
+    red[0][threadIdx.x] = a;
+    red[1][threadIdx.x] = b;
+    __syncthreads();
+    for (int o = DBLK / 2; o > 0; o >>= 1) {
+      if (threadIdx.x < o) {
+        red[0][threadIdx.x] += red[0][threadIdx.x + o];
+        red[1][threadIdx.x] += red[1][threadIdx.x + o];
+      }
+      __syncthreads();
+    }
+    if (threadIdx.x == 0) {
+      partial[((int64_t)blockIdx.x * nslot + s) * 2] = red[0][0];
+      partial[((int64_t)blockIdx.x * nslot + s) * 2 + 1] = red[1][0];
+    }
+    __syncthreads();
+  }
+}
+
+struct SlotScale {
+  double dot, inv_ne, inv_nd, sign;
+};
+
+// training samples from the captured slots: target g = (e/|e|)/(d/|d|) aligned
+// with d and clipped to [-4, 4], weight N (d/|d|)^2; every `stride`-th row
+__global__ void k_capture_samples(const double* cf, int nsd, int nst, const float* cX, const float* cd, const float* cc,
+                                  int nslot, int64_t N, const SlotScale* sc, int64_t stride, int64_t per_slot, float* X,
+                                  float* G, float* W) {
+  const int64_t total = (int64_t)nslot * per_slot;
+  for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < total; t += (int64_t)gridDim.x * blockDim.x) {
+    const int s = (int)(t / per_slot);
+    const int64_t r = (t % per_slot) * stride;
+    const int k = s % nst;
+    const SlotScale q = sc[s];
+    const double c = cc[(int64_t)s * N + r], d = cd[(int64_t)s * N + r];
+    const double e = cf[r * nsd + k] - q.dot * c;
+    const double dn = d * q.inv_nd, en = q.sign * e * q.inv_ne;
+    double g = 1.0, w = 0.0;
+    if (fabs(dn) > 1e-12) {
+      g = fmin(4.0, fmax(-4.0, en / dn));
+      w = (double)N * dn * dn;
+    }
+    for (int i = 0; i < QP_MLP_IN; ++i) X[t * QP_MLP_IN + i] = cX[((int64_t)s * N + r) * QP_MLP_IN + i];
+    G[t] = (float)g;
+    W[t] = (float)w;
   }
 }
 
@@ -272,7 +440,8 @@ struct Dav {
   double *U = nullptr, *W = nullptr, *S = nullptr, *R = nullptr;  // itermax blocks; R: one block
   float* u32 = nullptr;
   double* part = nullptr;  // gram / step partials
-  double* small = nullptr;  // device small matrices (MAXM*MAXS x 4)
+  double* small = nullptr;  // device small matrices (MAXM*MAXS x 6)
+  float *cX = nullptr, *cd = nullptr, *cc = nullptr;  // training capture
   int ncta = 0;
   int64_t rows_per_cta = 0;
   ~Dav() {
@@ -283,19 +452,23 @@ struct Dav {
     dev_free(u32);
     dev_free(part);
     dev_free(small);
+    dev_free(cX);
+    dev_free(cd);
+    dev_free(cc);
   }
   double* blk(double* X, int b) const { return X + (int64_t)b * N * nsd; }
 };
 
-int gram(Dav& d, const double* A, int m, const double* B, double* out_dev) {
-  const size_t shm = (size_t)GTR * (m + d.nsd) * sizeof(double);
-  k_gram<<<d.ncta, DBLK, shm, d.st>>>(A, m, B, d.nsd, d.N, d.rows_per_cta, d.part);
+int gram(Dav& d, const double* A, int m, const double* B, double* out_dev, const int* skip = nullptr) {
+  const int groups = DBLK / m;
+  const size_t shm = std::max((size_t)GTR * (m + d.nsd), (size_t)groups * m * d.nsd) * sizeof(double);
+  k_gram<<<d.ncta, DBLK, shm, d.st>>>(A, m, B, d.nsd, d.N, d.rows_per_cta, d.part, skip);
   k_reduce_partials<<<gsz(m * d.nsd), DBLK, 0, d.st>>>(d.part, d.ncta, m * d.nsd, out_dev);
   return 0;
 }
 
 void lincomb(Dav& d, int m, const double* C, int sub, const double* A0, double* O0, const double* A1 = nullptr,
-             double* O1 = nullptr, const double* A2 = nullptr, double* O2 = nullptr) {
+             double* O1 = nullptr, const double* A2 = nullptr, double* O2 = nullptr, const int* skip = nullptr) {
   LinComb L{};
   L.A[0] = A0;
   L.out[0] = O0;
@@ -310,21 +483,28 @@ void lincomb(Dav& d, int m, const double* C, int sub, const double* A0, double* 
     L.out[2] = O2;
     L.n = 3;
   }
-  k_lincomb<<<gsz(d.N), DBLK, 0, d.st>>>(L, m, d.nsd, d.N, C, sub);
+  k_lincomb<<<gsz(d.N), DBLK, 0, d.st>>>(L, m, d.nsd, d.N, C, sub, skip);
 }
 
-// orthonormalise block b against blocks 0..b-1 (CGS2) and within itself (CholQR2)
+// orthonormalise block b against blocks 0..b-1 (classical Gram-Schmidt, a
+// second pass when the first lost more than half of a column's norm) and
+// within itself (CholQR2)
 void orthonormalise(Dav& d, int b) {
   double* Ub = d.blk(d.U, b);
   double* cbuf = d.small;  // m x nsd
-  if (b > 0) {
-    for (int pass = 0; pass < 2; ++pass) {
-      gram(d, d.U, b * d.nsd, Ub, cbuf);
-      lincomb(d, b * d.nsd, cbuf, 1, d.U, Ub);
-    }
-  }
   double* G = d.small + MAXM * MAXS;
   double* Rinv = d.small + 2 * MAXM * MAXS;
+  double* G0 = d.small + 4 * MAXM * MAXS;
+  int* skip = (int*)(d.small + 5 * MAXM * MAXS);
+  if (b > 0) {
+    gram(d, Ub, d.nsd, Ub, G0);
+    gram(d, d.U, b * d.nsd, Ub, cbuf);
+    lincomb(d, b * d.nsd, cbuf, 1, d.U, Ub);
+    gram(d, Ub, d.nsd, Ub, G);
+    k_need_second_pass<<<1, 1, 0, d.st>>>(G0, G, d.nsd, skip);
+    gram(d, d.U, b * d.nsd, Ub, cbuf, skip);
+    lincomb(d, b * d.nsd, cbuf, 1, d.U, Ub, nullptr, nullptr, nullptr, nullptr, skip);
+  }
   for (int pass = 0; pass < 2; ++pass) {
     gram(d, Ub, d.nsd, Ub, G);
     k_chol_inv<<<1, 1, 0, d.st>>>(G, d.nsd, Rinv);
@@ -364,11 +544,35 @@ extern "C" int qpgpu_davidson_hs2(qpgpu_ctx* c, double* u_in, int64_t dim_in, do
   if (dev_alloc(&d.U, blkn * itermax) != cudaSuccess || dev_alloc(&d.W, blkn * itermax) != cudaSuccess ||
       dev_alloc(&d.S, blkn * itermax) != cudaSuccess || dev_alloc(&d.R, blkn) != cudaSuccess ||
       dev_alloc(&d.u32, blkn) != cudaSuccess || dev_alloc(&d.part, (size_t)d.ncta * MAXM * MAXS) != cudaSuccess ||
-      dev_alloc(&d.small, (size_t)4 * MAXM * MAXS) != cudaSuccess) {
+      dev_alloc(&d.small, (size_t)6 * MAXM * MAXS) != cudaSuccess) {
     cudaGetLastError();
     return qpgpu_fail(c, QPGPU_ERR_NOMEM, "Davidson work arrays do not fit on the device");
   }
   cudaStream_t st = d.st;
+  // learned preconditioner and training capture
+  const bool use_mlp = prm->preconditioner == 1;
+  if (use_mlp && (!c->mlp.ready || !c->d_detfeat))
+    return qpgpu_fail(c, QPGPU_ERR_STATE, "learned preconditioner requested but the MLP is not initialised");
+  bool mlp_on[MAXS] = {false};
+  int strikes[MAXS] = {0};
+  double prev_res[MAXS];
+  for (int k = 0; k < MAXS; ++k) prev_res[k] = INFINITY;
+  for (int k = 0; k < nst; ++k) mlp_on[k] = use_mlp;
+  int n_fallback = 0;
+  const int collect_every = prm->collect_every > 0 ? prm->collect_every : 0;
+  const int collect_max = collect_every ? std::max(1, std::min(prm->collect_max > 0 ? prm->collect_max : 8, 64 / nst)) : 0;
+  int n_cap = 0, it_global = 0;
+  int64_t n_new_samples = 0;
+  if (collect_every) {
+    if (!c->d_detfeat) return qpgpu_fail(c, QPGPU_ERR_STATE, "no determinant features");
+    const size_t nsl = (size_t)collect_max * nst;
+    if (cudaMalloc((void**)&d.cX, nsl * N * QP_MLP_IN * sizeof(float)) != cudaSuccess ||
+        cudaMalloc((void**)&d.cd, nsl * N * sizeof(float)) != cudaSuccess ||
+        cudaMalloc((void**)&d.cc, nsl * N * sizeof(float)) != cudaSuccess) {
+      cudaGetLastError();
+      return qpgpu_fail(c, QPGPU_ERR_NOMEM, "training capture does not fit on the device");
+    }
+  }
   cudaEvent_t ev0;
   QP_CUDA(c, cudaEventCreate(&ev0));
   std::vector<cudaEvent_t> evs;
@@ -482,7 +686,20 @@ extern "C" int qpgpu_davidson_hs2(qpgpu_ctx* c, double* u_in, int64_t dim_in, do
       sp.sz2sz = sz2sz;
       sp.nsd = nsd;
       sp.nst = nst;
-      k_step<<<d.ncta, DBLK, 0, st>>>(d.blk(d.U, iter), d.blk(d.W, iter), d.blk(d.S, iter), c->d_hdiag, N, sp, d.part);
+      ++it_global;
+      if (collect_every && n_cap < collect_max && it_global >= 2 && (it_global - 2) % collect_every == 0) {
+        k_capture<<<gsz(N), DBLK, 0, st>>>(d.blk(d.U, iter), d.blk(d.W, iter), d.blk(d.S, iter), c->d_hdiag,
+                                           (const float4*)c->d_detfeat, N, sp, n_cap * nst, d.cX, d.cd, d.cc);
+        ++n_cap;
+      }
+      unsigned mask = 0;
+      for (int k = 0; k < nst; ++k)
+        if (mlp_on[k]) mask |= 1u << k;
+      if (mask)
+        k_step_mlp<<<d.ncta, DBLK, 0, st>>>(d.blk(d.U, iter), d.blk(d.W, iter), d.blk(d.S, iter), c->d_hdiag,
+                                            (const float4*)c->d_detfeat, c->mlp.params, N, sp, mask, d.part);
+      else
+        k_step<<<d.ncta, DBLK, 0, st>>>(d.blk(d.U, iter), d.blk(d.W, iter), d.blk(d.S, iter), c->d_hdiag, N, sp, d.part);
       QP_CUDA(c, cudaGetLastError());
       QP_CUDA(c, cudaMemcpyAsync(partial.data(), d.part, partial.size() * sizeof(double), cudaMemcpyDeviceToHost, st));
       QP_CUDA(c, cudaStreamSynchronize(st));
@@ -493,6 +710,19 @@ extern "C" int qpgpu_davidson_hs2(qpgpu_ctx* c, double* u_in, int64_t dim_in, do
         res[k] = r;
         mx = std::max(mx, r);
         if (r > 1e8 || !std::isfinite(r)) failed = true;  // 'Davidson failed' (:404-409)
+      }
+      // fallback: a state whose residual (the reference's measure, from the
+      // diagonal correction) grew in two consecutive learned steps goes back
+      // to the diagonal step for the rest of the run
+      for (int k = 0; k < nst; ++k) {
+        if (mlp_on[k]) {
+          strikes[k] = (res[k] > prev_res[k]) ? strikes[k] + 1 : 0;
+          if (strikes[k] >= 2) {
+            mlp_on[k] = false;
+            ++n_fallback;
+          }
+        }
+        prev_res[k] = res[k];
       }
       record(prec);
       if (failed) break;
@@ -519,6 +749,63 @@ extern "C" int qpgpu_davidson_hs2(qpgpu_ctx* c, double* u_in, int64_t dim_in, do
       for (int j = 0; j < mmax; ++j) h[(size_t)i * mmax + j] = s_[(size_t)i * mmax + j] = 0.0;
   }
   QP_CUDA(c, cudaGetLastError());
+  // training pairs from the captured iterations, with the final vectors
+  if (n_cap > 0 && !failed) {
+    const int nslot = n_cap * nst;
+    std::vector<double> part((size_t)d.ncta * nslot * 2), dot(nslot, 0.0), nd(nslot, 0.0), ne(nslot, 0.0),
+        ed(nslot, 0.0);
+    double* dpart = nullptr;
+    double* ddot = nullptr;
+    SlotScale* dsc = nullptr;
+    QP_CUDA(c, cudaMalloc((void**)&dpart, part.size() * sizeof(double)));
+    QP_CUDA(c, cudaMalloc((void**)&ddot, nslot * sizeof(double)));
+    QP_CUDA(c, cudaMalloc((void**)&dsc, nslot * sizeof(SlotScale)));
+    k_capture_sums<<<d.ncta, DBLK, 0, st>>>(d.U, nsd, nst, d.cd, d.cc, nslot, N, nullptr, 0, dpart);
+    QP_CUDA(c, cudaMemcpyAsync(part.data(), dpart, part.size() * sizeof(double), cudaMemcpyDeviceToHost, st));
+    QP_CUDA(c, cudaStreamSynchronize(st));
+    for (int q = 0; q < d.ncta; ++q)
+      for (int sl = 0; sl < nslot; ++sl) {
+        dot[sl] += part[((size_t)q * nslot + sl) * 2];
+        nd[sl] += part[((size_t)q * nslot + sl) * 2 + 1];
+      }
+    QP_CUDA(c, cudaMemcpyAsync(ddot, dot.data(), nslot * sizeof(double), cudaMemcpyHostToDevice, st));
+    k_capture_sums<<<d.ncta, DBLK, 0, st>>>(d.U, nsd, nst, d.cd, d.cc, nslot, N, ddot, 1, dpart);
+    QP_CUDA(c, cudaMemcpyAsync(part.data(), dpart, part.size() * sizeof(double), cudaMemcpyDeviceToHost, st));
+    QP_CUDA(c, cudaStreamSynchronize(st));
+    for (int q = 0; q < d.ncta; ++q)
+      for (int sl = 0; sl < nslot; ++sl) {
+        ne[sl] += part[((size_t)q * nslot + sl) * 2];
+        ed[sl] += part[((size_t)q * nslot + sl) * 2 + 1];
+      }
+    std::vector<SlotScale> sc(nslot);
+    for (int sl = 0; sl < nslot; ++sl) {
+      const bool ok = ne[sl] > 1e-30 && nd[sl] > 1e-300;
+      sc[sl].dot = dot[sl];
+      sc[sl].inv_ne = ok ? 1.0 / std::sqrt(ne[sl]) : 0.0;
+      sc[sl].inv_nd = ok ? 1.0 / std::sqrt(nd[sl]) : 0.0;
+      sc[sl].sign = ed[sl] >= 0 ? 1.0 : -1.0;
+    }
+    QP_CUDA(c, cudaMemcpyAsync(dsc, sc.data(), nslot * sizeof(SlotScale), cudaMemcpyHostToDevice, st));
+    const int64_t per_cap = 32768;
+    const int64_t stride = std::max<int64_t>(1, (N + per_cap - 1) / per_cap);
+    const int64_t per_slot = (N + stride - 1) / stride;
+    const int64_t total = per_slot * nslot;
+    float *X = nullptr, *Gt = nullptr, *Wt = nullptr;
+    QP_CUDA(c, cudaMalloc((void**)&X, total * QP_MLP_IN * sizeof(float)));
+    QP_CUDA(c, cudaMalloc((void**)&Gt, total * sizeof(float)));
+    QP_CUDA(c, cudaMalloc((void**)&Wt, total * sizeof(float)));
+    k_capture_samples<<<gsz(total), DBLK, 0, st>>>(d.U, nsd, nst, d.cX, d.cd, d.cc, nslot, N, dsc, stride, per_slot, X,
+                                                   Gt, Wt);
+    int rc2 = qp_mlp_append(c, X, Gt, Wt, total, true);
+    cudaFree(X);
+    cudaFree(Gt);
+    cudaFree(Wt);
+    cudaFree(dpart);
+    cudaFree(ddot);
+    cudaFree(dsc);
+    if (rc2) return rc2;
+    n_new_samples = total;
+  }
   // final vectors (block 0 after re-contraction) back to psi_det order
   {
     double* hstage = nullptr;
@@ -543,6 +830,8 @@ extern "C" int qpgpu_davidson_hs2(qpgpu_ctx* c, double* u_in, int64_t dim_in, do
     }
     trace->n_sigma = n_sigma;
     trace->converged = converged ? 1 : 0;
+    trace->n_fallback = n_fallback;
+    trace->n_samples = n_new_samples;
   }
   cudaEventDestroy(ev0);
   if (failed) return qpgpu_fail(c, QPGPU_ERR_DAVIDSON, "Davidson failed: residual above 1e8");

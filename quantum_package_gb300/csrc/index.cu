@@ -352,7 +352,8 @@ void qp_free_dets(qpgpu_ctx* c) {
   void** ps[] = {(void**)&c->d_dets, (void**)&c->d_alpha, (void**)&c->d_beta, (void**)&c->d_rows,
                  (void**)&c->d_cols, (void**)&c->d_order, (void**)&c->d_col_loc, (void**)&c->d_t_order,
                  (void**)&c->d_t_cols, (void**)&c->d_row_loc, (void**)&c->d_sa_ptr, (void**)&c->d_sa_idx,
-                 (void**)&c->d_sb_ptr, (void**)&c->d_sb_idx, (void**)&c->d_cost_a, (void**)&c->d_cost_b};
+                 (void**)&c->d_sb_ptr, (void**)&c->d_sb_idx, (void**)&c->d_cost_a, (void**)&c->d_cost_b,
+                 (void**)&c->d_detfeat};
   for (auto p : ps) {
     dev_free(*p);
     *p = nullptr;

@@ -317,6 +317,40 @@ struct SigmaItems {
   }
 };
 
+// Learned preconditioner: MLP 8 -> 64 -> 64 -> 1 (GELU), FP32 parameters
+// packed as W1[64][8], b1[64], W2[64][64], b2[64], W3[64], b3.
+#define QP_MLP_IN 8
+#define QP_MLP_H 64
+#define QP_MLP_W1 0
+#define QP_MLP_B1 (QP_MLP_W1 + QP_MLP_H * QP_MLP_IN)
+#define QP_MLP_W2 (QP_MLP_B1 + QP_MLP_H)
+#define QP_MLP_B2 (QP_MLP_W2 + QP_MLP_H * QP_MLP_H)
+#define QP_MLP_W3 (QP_MLP_B2 + QP_MLP_H)
+#define QP_MLP_B3 (QP_MLP_W3 + QP_MLP_H)
+#define QP_MLP_NPARAM (QP_MLP_B3 + 1)
+
+struct MlpState {
+  float* params = nullptr;  // device
+  float* adam_m = nullptr;
+  float* adam_v = nullptr;
+  int64_t adam_t = 0;
+  bool ready = false;
+  // training set: features X[n][8], target multiplier G[n], weight Wt[n]
+  float* X = nullptr;
+  float* G = nullptr;
+  float* Wt = nullptr;
+  int64_t n = 0, cap = 0;
+  void free_all() {
+    void* ps[] = {params, adam_m, adam_v, X, G, Wt};
+    for (void* p : ps)
+      if (p) cudaFree(p);
+    params = adam_m = adam_v = X = G = Wt = nullptr;
+    n = cap = 0;
+    adam_t = 0;
+    ready = false;
+  }
+};
+
 struct qpgpu_ctx {
   std::mutex mu;
   int device = 0;
@@ -369,6 +403,8 @@ struct qpgpu_ctx {
   float* d_hdiag32 = nullptr;
   double setup_ms = 0.0;
   SigmaItems items;
+  MlpState mlp;
+  float* d_detfeat = nullptr;  // (N, 4): alpha rank, beta rank, orbital-energy sum, open shells
   // optional phase timing of the set-up (environment QPGPU_PROFILE=1)
   bool profile = false;
   std::vector<std::pair<std::string, cudaEvent_t>> marks;
@@ -420,3 +456,43 @@ inline void qp_mark(qpgpu_ctx* c, const char* name) {
   c->marks.emplace_back(name, e);
 }
 void qp_report_marks(qpgpu_ctx* c);  // ctx.cu
+
+// learned preconditioner (mlp.cu)
+int qp_det_features(qpgpu_ctx* c);
+int qp_mlp_append(qpgpu_ctx* c, const float* X, const float* G, const float* W, int64_t n, bool device_src);
+#ifdef __CUDACC__
+__device__ __forceinline__ float qp_gelu(float x) { return 0.5f * x * (1.0f + erff(x * 0.70710678118654752f)); }
+__device__ __forceinline__ float qp_gelu_grad(float x) {
+  return 0.5f * (1.0f + erff(x * 0.70710678118654752f)) + x * 0.39894228040143268f * expf(-0.5f * x * x);
+}
+// features of one (determinant, state): static (N,4) features + dynamic ones
+__device__ __forceinline__ void qp_features(const float4 st, double hmL, double c, double r, double d, float* f) {
+  f[0] = st.x * 0.25f;
+  f[1] = st.y * 0.25f;
+  f[2] = (float)(hmL * 0.1);
+  f[3] = st.z * 0.1f;
+  f[4] = st.w * 0.125f;
+  f[5] = (float)(log10(fabs(c) + 1e-30) / 8.0);
+  f[6] = (float)(log10(fabs(r) + 1e-30) / 8.0);
+  f[7] = (float)(log10(fabs(d) + 1e-30) / 8.0);
+}
+// forward pass with the parameters in shared memory
+__device__ __forceinline__ float qp_mlp_forward(const float* P, const float* f) {
+  float h1[QP_MLP_H];
+#pragma unroll 8
+  for (int j = 0; j < QP_MLP_H; ++j) {
+    float a = P[QP_MLP_B1 + j];
+#pragma unroll
+    for (int i = 0; i < QP_MLP_IN; ++i) a = fmaf(P[QP_MLP_W1 + j * QP_MLP_IN + i], f[i], a);
+    h1[j] = qp_gelu(a);
+  }
+  float y = P[QP_MLP_B3];
+  for (int j = 0; j < QP_MLP_H; ++j) {
+    float a = P[QP_MLP_B2 + j];
+#pragma unroll 16
+    for (int i = 0; i < QP_MLP_H; ++i) a = fmaf(P[QP_MLP_W2 + j * QP_MLP_H + i], h1[i], a);
+    y = fmaf(P[QP_MLP_W3 + j], qp_gelu(a), y);
+  }
+  return y;
+}
+#endif

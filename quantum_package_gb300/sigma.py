@@ -153,18 +153,21 @@ class Wavefunction:
 
     # --- Davidson ------------------------------------------------------
     def davidson_diag_hs2(self, u_in, n_states, davidson_sze_max=8, threshold=1e-12, s2_eig=True,
-                          precision=FP64, defect_every=0, preconditioner=0, max_iter=500, trace_cap=512):
+                          precision=FP64, defect_every=0, preconditioner=0, max_iter=500, collect_every=0,
+                          collect_max=8, trace_cap=1024):
         """davidson_diag_hs2 (diagonalization_hs2.irp.f:1-49) on this determinant set.
 
         u_in: (N_st_diag, N) guess vectors (all of them, seeded by the caller).
-        Returns dict(energies, s2, vectors, n_sigma, trace) with electronic energies.
+        preconditioner=1 uses the learned step (see mlp_*); collect_every > 0
+        captures training pairs for it.  Returns dict(energies, s2, vectors,
+        n_sigma, converged, n_fallback, n_samples, trace) with electronic energies.
         """
         u = np.ascontiguousarray(np.atleast_2d(u_in), dtype=np.float64).copy()
         nsd, n = u.shape
         prm = _lib.DavidsonParams(n_states=n_states, n_states_diag=nsd, davidson_sze_max=davidson_sze_max,
                                   s2_eig=int(bool(s2_eig)), threshold=threshold, precision=precision,
                                   defect_every=defect_every, preconditioner=preconditioner, max_iter=max_iter,
-                                  energy_tol=0.0)
+                                  collect_every=collect_every, collect_max=collect_max)
         prec = np.zeros(trace_cap, np.int32)
         en = np.zeros((trace_cap, n_states))
         rs = np.zeros((trace_cap, n_states))
@@ -178,5 +181,52 @@ class Wavefunction:
             check(rc, self._ctx)
         k = tr.n
         return dict(energies=e, s2=s2, vectors=u, n_sigma=rc, converged=bool(tr.converged),
+                    n_fallback=tr.n_fallback, n_samples=tr.n_samples,
                     trace=dict(precision=prec[:k].copy(), energies=en[:k].copy(), residuals=rs[:k].copy(),
                                elapsed_ms=el[:k].copy()))
+
+    # --- learned preconditioner -----------------------------------------
+    def mlp_init(self, seed=0):
+        check(_lib.load().qpgpu_mlp_init(self._ctx, seed), self._ctx)
+
+    def mlp_weights(self):
+        w = np.empty(_lib.MLP_NPARAM, np.float32)
+        check(_lib.load().qpgpu_mlp_get_weights(self._ctx, _p(w)), self._ctx)
+        return w
+
+    def mlp_set_weights(self, w):
+        w = np.ascontiguousarray(w, np.float32)
+        check(_lib.load().qpgpu_mlp_set_weights(self._ctx, _p(w)), self._ctx)
+
+    def mlp_add_samples(self, X, g, w):
+        X = np.ascontiguousarray(X, np.float32)
+        g = np.ascontiguousarray(g, np.float32)
+        w = np.ascontiguousarray(w, np.float32)
+        check(_lib.load().qpgpu_mlp_add_samples(self._ctx, _p(X), _p(g), _p(w), len(g)), self._ctx)
+
+    def mlp_clear_samples(self):
+        check(_lib.load().qpgpu_mlp_clear_samples(self._ctx), self._ctx)
+
+    def mlp_n_samples(self):
+        return _lib.load().qpgpu_mlp_n_samples(self._ctx)
+
+    def mlp_gradient(self, X, g, w):
+        X = np.ascontiguousarray(X, np.float32)
+        g = np.ascontiguousarray(g, np.float32)
+        w = np.ascontiguousarray(w, np.float32)
+        grad = np.empty(_lib.MLP_NPARAM, np.float32)
+        loss = C.c_float()
+        check(_lib.load().qpgpu_mlp_gradient(self._ctx, _p(X), _p(g), _p(w), len(g), _p(grad), C.byref(loss)),
+              self._ctx)
+        return grad, loss.value
+
+    def mlp_predict(self, X):
+        X = np.ascontiguousarray(X, np.float32)
+        y = np.empty(len(X), np.float32)
+        check(_lib.load().qpgpu_mlp_predict(self._ctx, _p(X), len(X), _p(y)), self._ctx)
+        return y
+
+    def mlp_train(self, epochs=20, batch=4096, lr=1e-3, seed=0):
+        loss = C.c_float()
+        check(_lib.load().qpgpu_mlp_train(self._ctx, epochs, batch, lr, seed, C.byref(loss)), self._ctx)
+        return loss.value
