@@ -51,6 +51,8 @@ def parse():
     ap.add_argument("--cpu-sample-step", type=int, default=250,
                     help="row stride of the CPU-oracle sample (1/step of the rows)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-davidson", action="store_true", help="skip the Davidson time-to-E block")
+    ap.add_argument("--davidson-only", action="store_true", help="only the Davidson block (profiling)")
     return ap.parse_args()
 
 
@@ -193,6 +195,75 @@ def workload_config(prob):
             "l2": "inputs larger than L2 (stored pairs ~12 GB FP64 per sigma)"}
 
 
+N_STATES_DIAG = 8
+E_TOL = 1e-6
+
+
+def _guess(n, seed):
+    """Unit vector on the reference determinant + seeded Gaussian extra vectors."""
+    rng = np.random.default_rng(seed)
+    u = rng.normal(size=(N_STATES_DIAG, n))
+    u[0] = 0.0
+    u[0, 0] = 1.0
+    return u
+
+
+def _time_to_e(res, e_ref, fp64):
+    """ms from the Davidson call until an FP64-sigma iteration has every state within E_TOL of e_ref."""
+    tr = res["trace"]
+    de = np.abs(tr["energies"] - e_ref[None, :]).max(axis=1)
+    ok = np.where((de < E_TOL) & (tr["precision"] == fp64))[0]
+    return (float(tr["elapsed_ms"][ok[0]]) if len(ok) else None), int(ok[0] + 1) if len(ok) else None
+
+
+def davidson_block(prob, wf):
+    """Time-to-E of the 4 lowest states: plain FP64 Davidson vs mixed precision vs
+    mixed precision + learned preconditioner (trained on the first 1e4 and 2e5
+    determinants of the same draw, as earlier CIPSI stages)."""
+    from quantum_package_gb300 import FP32, FP64
+    N = prob.n_det
+    u = _guess(N, prob.seed)
+    kw = dict(n_states=N_STATES, s2_eig=False, max_iter=400)
+    tight = wf.davidson_diag_hs2(u, threshold=1e-12, **kw)
+    e_ref = tight["energies"][:N_STATES]
+    out = {"n_states": N_STATES, "n_states_diag": N_STATES_DIAG, "threshold": 1e-10, "e_tol_ha": E_TOL,
+           "fp64_reference_energies": e_ref.tolist(),
+           "note": "s2_eig off: the seeded space is not spin complete; energies are electronic (Ha)"}
+
+    def run(name, **extra):
+        r = wf.davidson_diag_hs2(u, threshold=1e-10, **kw, **extra)
+        t, it = _time_to_e(r, e_ref, FP64)
+        out[name] = {"time_to_E_s": t / 1e3 if t is not None else None, "iterations_to_E": it,
+                     "n_sigma": r["n_sigma"], "converged": r["converged"],
+                     "total_s": float(r["trace"]["elapsed_ms"][-1]) / 1e3,
+                     "max_dE_ha": float(np.abs(r["energies"][:N_STATES] - e_ref).max()),
+                     "n_fallback": r["n_fallback"]}
+        return r
+
+    run("plain_fp64")
+    run("mixed", precision=FP32)
+    # learned preconditioner: earlier stages of the same determinant draw
+    t0 = time.perf_counter()
+    wf.mlp_init(seed=3)
+    train = {}
+    for n_stage in (10_000, 200_000):
+        if n_stage >= N:
+            continue
+        wf.set_dets(prob.dets[:n_stage])
+        r = wf.davidson_diag_hs2(_guess(n_stage, prob.seed), threshold=1e-10, collect_every=1, collect_max=16,
+                                 preconditioner=1 if train else 0, **kw)
+        loss = wf.mlp_train(epochs=20, batch=4096, lr=2e-3, seed=4)
+        train[str(n_stage)] = {"n_sigma": r["n_sigma"], "samples": int(r["n_samples"]), "loss": loss}
+    wf.set_dets(prob.dets)
+    out["training"] = {"stages": train, "wall_s": time.perf_counter() - t0,
+                       "note": "training on earlier determinant sets; not part of time-to-E"}
+    run("plain_fp64_learned", preconditioner=1)
+    run("mixed_learned", precision=FP32, preconditioner=1)
+    a, b = out["plain_fp64"]["time_to_E_s"], out["mixed_learned"]["time_to_E_s"]
+    out["speedup_mixed_learned_vs_plain"] = (a / b) if (a and b) else None
+    return out
+
+
 def run_ours(args):
     import torch
     rank, world, local = dist_env()
@@ -217,6 +288,11 @@ def run_ours(args):
     wf = Wavefunction.from_problem(prob)
     info = wf.info()
     P = info["n_pairs"]
+    if args.davidson_only:
+        d = davidson_block(prob, wf)
+        if rank == 0:
+            print(json.dumps({"davidson": d, "setup_s": info["setup_ms"] / 1e3}), flush=True)
+        return 0
     dev = torch.device("cuda", local)
     stream = torch.cuda.Stream(device=dev)
     order = torch.from_numpy(wf.bilinear_order().astype(np.int64)).to(dev)
@@ -306,6 +382,8 @@ def run_ours(args):
         "gpu_launches": launches_per_sigma * args.steps,
         "clocks": clk.summary(),
     }
+    if not args.no_davidson:
+        line["davidson"] = davidson_block(prob, wf)
     if cpu:
         line["cpu_baseline"] = cpu
     if traffic is not None:

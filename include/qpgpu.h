@@ -172,7 +172,7 @@ int qpgpu_davidson_hs2(qpgpu_ctx* ctx, double* u_in, int64_t dim_in, double* ene
  * W2[64][64], b2[64], W3[64], b3) that scales the diagonal correction of the
  * Davidson step per determinant.  Features (8 floats): alpha and beta
  * excitation rank / 4, (H_II - E)/10, hole/particle orbital-energy sum / 10,
- * open shells / 8, log10|c_I|/8, log10|r_I|/8, log10|d_I|/8.  Samples are
+ * log10(sum_J H_IJ^2)/4, log10|c_I|/8, log10|r_I|/8, log10|d_I|/8.  Samples are
  * (features, target multiplier g, weight w); the loss is mean(w (y - g)^2).
  * The training set and the parameters belong to the context and survive
  * qpgpu_set_dets (earlier determinant sets train later ones). */

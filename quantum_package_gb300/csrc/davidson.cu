@@ -42,30 +42,34 @@ inline unsigned gsz(int64_t n, int tpb = DBLK) {
 
 // G[i][j] = sum_r A_i[r] B_j[r] for the m columns of A (stacked blocks of nsd
 // columns, block stride N*nsd) and the nsd columns of B.  Rows are staged in
-// shared memory; thread t owns column i = t % m of A for every j (register
-// tile of nsd accumulators) over the rows r = t / m (mod 256 / m) of the tile,
-// and the row groups are added in a fixed order.  One partial per CTA.
-// A non-null `skip` flag that is set makes the kernel write zeros (used for
-// the conditional second Gram-Schmidt pass).
+// shared memory; a thread owns CI consecutive columns of A for every j (a
+// CI x nsd register tile: CI + nsd shared reads per CI*nsd FMAs) over the rows
+// of its row group, and the row groups are added in a fixed order.  One
+// partial per CTA.  A non-null `skip` flag that is set makes the kernel write
+// zeros (the conditional second Gram-Schmidt pass).
 constexpr int GTR = 32;
+template <int CI>
 __global__ void __launch_bounds__(DBLK) k_gram(const double* A, int m, const double* B, int nsd, int64_t N,
                                                int64_t rows_per_cta, double* partial, const int* skip) {
   extern __shared__ double sm[];
-  double* As = sm;                 // [GTR][m]
-  double* Bs = sm + GTR * m;       // [GTR][nsd]
+  double* As = sm;            // [GTR][m]
+  double* Bs = sm + GTR * m;  // [GTR][nsd]
   const int np = m * nsd;
+  const int ncol = m / CI;                       // column groups
+  const int groups = min(DBLK / ncol, GTR);      // row groups
   if (skip && *skip) {
     for (int p = threadIdx.x; p < np; p += DBLK) partial[(int64_t)blockIdx.x * np + p] = 0.0;
     return;
   }
   const int64_t r0 = (int64_t)blockIdx.x * rows_per_cta;
   const int64_t r1 = min(r0 + rows_per_cta, N);
-  const int groups = DBLK / m;  // m <= 128 -> at least 2 groups
-  const int i = threadIdx.x % m, g = threadIdx.x / m;
+  const int ci = threadIdx.x % ncol, g = threadIdx.x / ncol;
   const bool active = g < groups;
-  double acc[MAXS];
+  double acc[CI][MAXS];
 #pragma unroll
-  for (int j = 0; j < MAXS; ++j) acc[j] = 0.0;
+  for (int a = 0; a < CI; ++a)
+#pragma unroll
+    for (int j = 0; j < MAXS; ++j) acc[a][j] = 0.0;
   for (int64_t t0 = r0; t0 < r1; t0 += GTR) {
     const int tr = (int)min((int64_t)GTR, r1 - t0);
     __syncthreads();
@@ -78,19 +82,28 @@ __global__ void __launch_bounds__(DBLK) k_gram(const double* A, int m, const dou
     __syncthreads();
     if (active) {
       for (int r = g; r < tr; r += groups) {
-        const double a = As[r * m + i];
+        double a[CI];
+#pragma unroll
+        for (int q = 0; q < CI; ++q) a[q] = As[r * m + ci * CI + q];
         const double* brow = &Bs[r * nsd];
 #pragma unroll
-        for (int j = 0; j < MAXS; ++j)
-          if (j < nsd) acc[j] = fma(a, brow[j], acc[j]);
+        for (int j = 0; j < MAXS; ++j) {
+          if (j < nsd) {
+            const double bv = brow[j];
+#pragma unroll
+            for (int q = 0; q < CI; ++q) acc[q][j] = fma(a[q], bv, acc[q][j]);
+          }
+        }
       }
     }
   }
   __syncthreads();
-  // fixed-order sum over row groups through shared memory (reuses As)
+  // fixed-order sum over row groups through shared memory (reuses the tiles)
   double* red = sm;  // [groups][m][nsd]
   if (active)
-    for (int j = 0; j < nsd; ++j) red[((size_t)g * m + i) * nsd + j] = acc[j];
+#pragma unroll
+    for (int q = 0; q < CI; ++q)
+      for (int j = 0; j < nsd; ++j) red[((size_t)g * m + ci * CI + q) * nsd + j] = acc[q][j];
   __syncthreads();
   for (int p = threadIdx.x; p < np; p += DBLK) {
     double s = 0.0;
@@ -99,18 +112,26 @@ __global__ void __launch_bounds__(DBLK) k_gram(const double* A, int m, const dou
   }
 }
 
-// out[p] = sum over CTAs (in order) of partial[cta][p]
+// out[p] = sum over CTAs of partial[cta][p]: one warp per element, lane l
+// adds CTAs l, l+32, ... and the lanes combine in a fixed butterfly order
 __global__ void k_reduce_partials(const double* partial, int ncta, int np, double* out) {
-  for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < np; p += gridDim.x * blockDim.x) {
+  const int lane = threadIdx.x & 31;
+  const int wpb = blockDim.x >> 5;
+  for (int p = blockIdx.x * wpb + (threadIdx.x >> 5); p < np; p += gridDim.x * wpb) {
     double s = 0.0;
-    for (int c = 0; c < ncta; ++c) s += partial[(int64_t)c * np + p];
-    out[p] = s;
+    for (int c = lane; c < ncta; c += 32) s += partial[(int64_t)c * np + p];
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+    if (lane == 0) out[p] = s;
   }
 }
 
 // out_k[r][j] (=, -=) sum_i A_k[i-th column][r] C[i][j], for up to 3 (A, out)
-// pairs sharing C (m x nsd, row-major).  out may alias A when m == nsd (the
-// thread reads its whole row before writing it).
+// pairs sharing C (m x nsd, row-major).  Each thread owns LR rows (LR*256
+// apart, so a warp's loads stay contiguous) and keeps LR x nsd accumulators:
+// one shared-memory read of C serves LR FMAs.  out may alias A when m == nsd
+// (a thread reads all its rows before writing them).
+constexpr int LR = 4;
 struct LinComb {
   const double* A[3];
   double* out[3];
@@ -119,27 +140,50 @@ struct LinComb {
 __global__ void __launch_bounds__(DBLK) k_lincomb(LinComb L, int m, int nsd, int64_t N, const double* C, int sub,
                                                   const int* skip) {
   if (skip && *skip) return;
-  __shared__ double Cs[MAXM * MAXS];
+  __shared__ __align__(16) double Cs[MAXM * MAXS];
   for (int i = threadIdx.x; i < m * nsd; i += DBLK) Cs[i] = C[i];
   __syncthreads();
   const int nb = m / nsd;
-  for (int64_t r = blockIdx.x * (int64_t)DBLK + threadIdx.x; r < N; r += (int64_t)gridDim.x * DBLK) {
-    for (int t = 0; t < L.n; ++t) {
-      double acc[MAXS];
+  const int64_t span = (int64_t)DBLK * LR;
+  for (int64_t base = (int64_t)blockIdx.x * span; base < N; base += (int64_t)gridDim.x * span) {
+    int64_t rr[LR];
+    bool ok[LR];
 #pragma unroll
-      for (int j = 0; j < MAXS; ++j) acc[j] = 0.0;
+    for (int q = 0; q < LR; ++q) {
+      rr[q] = base + threadIdx.x + (int64_t)q * DBLK;
+      ok[q] = rr[q] < N;
+    }
+    for (int t = 0; t < L.n; ++t) {
+      double acc[LR][MAXS];
+#pragma unroll
+      for (int q = 0; q < LR; ++q)
+#pragma unroll
+        for (int j = 0; j < MAXS; ++j) acc[q][j] = 0.0;
       for (int b = 0; b < nb; ++b) {
-        const double* a = L.A[t] + (int64_t)b * N * nsd + r * nsd;
+        const double* ab = L.A[t] + (int64_t)b * N * nsd;
         for (int c = 0; c < nsd; ++c) {
-          const double x = a[c];
+          double x[LR];
+#pragma unroll
+          for (int q = 0; q < LR; ++q) x[q] = ok[q] ? ab[rr[q] * nsd + c] : 0.0;
           const double* crow = &Cs[(b * nsd + c) * nsd];
 #pragma unroll
-          for (int j = 0; j < MAXS; ++j)
-            if (j < nsd) acc[j] = fma(x, crow[j], acc[j]);
+          for (int j = 0; j < MAXS; ++j) {
+            if (j < nsd) {
+              const double cv = crow[j];
+#pragma unroll
+              for (int q = 0; q < LR; ++q) acc[q][j] = fma(x[q], cv, acc[q][j]);
+            }
+          }
         }
       }
-      double* o = L.out[t] + r * nsd;
-      for (int j = 0; j < nsd; ++j) o[j] = sub ? o[j] - acc[j] : acc[j];
+#pragma unroll
+      for (int q = 0; q < LR; ++q) {
+        if (!ok[q]) continue;
+        double* o = L.out[t] + rr[q] * nsd;
+#pragma unroll
+        for (int j = 0; j < MAXS; ++j)
+          if (j < nsd) o[j] = sub ? o[j] - acc[q][j] : acc[q][j];
+      }
     }
   }
 }
@@ -460,10 +504,23 @@ struct Dav {
 };
 
 int gram(Dav& d, const double* A, int m, const double* B, double* out_dev, const int* skip = nullptr) {
-  const int groups = DBLK / m;
+  const int ci = (m % 4 == 0) ? 4 : (m % 2 == 0) ? 2 : 1;
+  const int groups = std::min(DBLK / (m / ci), GTR);
   const size_t shm = std::max((size_t)GTR * (m + d.nsd), (size_t)groups * m * d.nsd) * sizeof(double);
-  k_gram<<<d.ncta, DBLK, shm, d.st>>>(A, m, B, d.nsd, d.N, d.rows_per_cta, d.part, skip);
-  k_reduce_partials<<<gsz(m * d.nsd), DBLK, 0, d.st>>>(d.part, d.ncta, m * d.nsd, out_dev);
+  static bool attr_set = false;  // shared memory above 48 KB needs an opt-in (at most 64 KB here)
+  if (!attr_set) {
+    cudaFuncSetAttribute(k_gram<4>, cudaFuncAttributeMaxDynamicSharedMemorySize, 96 * 1024);
+    cudaFuncSetAttribute(k_gram<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, 96 * 1024);
+    cudaFuncSetAttribute(k_gram<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, 96 * 1024);
+    attr_set = true;
+  }
+  if (ci == 4)
+    k_gram<4><<<d.ncta, DBLK, shm, d.st>>>(A, m, B, d.nsd, d.N, d.rows_per_cta, d.part, skip);
+  else if (ci == 2)
+    k_gram<2><<<d.ncta, DBLK, shm, d.st>>>(A, m, B, d.nsd, d.N, d.rows_per_cta, d.part, skip);
+  else
+    k_gram<1><<<d.ncta, DBLK, shm, d.st>>>(A, m, B, d.nsd, d.N, d.rows_per_cta, d.part, skip);
+  k_reduce_partials<<<gsz((int64_t)m * d.nsd * 32), DBLK, 0, d.st>>>(d.part, d.ncta, m * d.nsd, out_dev);
   return 0;
 }
 
@@ -483,7 +540,7 @@ void lincomb(Dav& d, int m, const double* C, int sub, const double* A0, double* 
     L.out[2] = O2;
     L.n = 3;
   }
-  k_lincomb<<<gsz(d.N), DBLK, 0, d.st>>>(L, m, d.nsd, d.N, C, sub, skip);
+  k_lincomb<<<gsz((d.N + LR - 1) / LR), DBLK, 0, d.st>>>(L, m, d.nsd, d.N, C, sub, skip);
 }
 
 // orthonormalise block b against blocks 0..b-1 (classical Gram-Schmidt, a
@@ -712,11 +769,11 @@ extern "C" int qpgpu_davidson_hs2(qpgpu_ctx* c, double* u_in, int64_t dim_in, do
         if (r > 1e8 || !std::isfinite(r)) failed = true;  // 'Davidson failed' (:404-409)
       }
       // fallback: a state whose residual (the reference's measure, from the
-      // diagonal correction) grew in two consecutive learned steps goes back
-      // to the diagonal step for the rest of the run
+      // diagonal correction) fell by less than 5% in two consecutive learned
+      // steps goes back to the diagonal step for the rest of the run
       for (int k = 0; k < nst; ++k) {
         if (mlp_on[k]) {
-          strikes[k] = (res[k] > prev_res[k]) ? strikes[k] + 1 : 0;
+          strikes[k] = (res[k] > 0.95 * prev_res[k]) ? strikes[k] + 1 : 0;
           if (strikes[k] >= 2) {
             mlp_on[k] = false;
             ++n_fallback;

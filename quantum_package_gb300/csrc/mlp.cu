@@ -28,20 +28,20 @@ inline unsigned gsz(int64_t n, int tpb = 256) {
 
 // static features of each determinant (bilinear order): excitation rank of the
 // alpha and beta strings relative to the reference, sum of h_pp over particles
-// minus holes (orbital-energy change), number of open shells
+// minus holes (orbital-energy change); .w is set by k_row_coupling
 template <int NINT>
 __global__ void k_det_features(DevTables t, const u64* alpha, const u64* beta, const int* rows, const int* cols,
                                float4* out, int64_t N) {
   for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < N; k += (int64_t)gridDim.x * blockDim.x) {
     const u64* a = alpha + (int64_t)rows[k] * NINT;
     const u64* b = beta + (int64_t)cols[k] * NINT;
-    int ra = 0, rb = 0, open = 0;
+    int ra = 0, rb = 0;
     double e = 0.0;
     for (int w = 0; w < NINT; ++w) {
       const u64 xa = a[w] ^ t.ref[w], xb = b[w] ^ t.ref[NINT + w];
       ra += popc64(xa);
       rb += popc64(xb);
-      open += popc64(a[w] ^ b[w]);
+
       for (u64 x = xa; x; x &= x - 1) {
         const int p = ctz64(x) + 1 + 64 * w;
         const double hp = tab2(t.h, t.n, p, p);
@@ -53,7 +53,22 @@ __global__ void k_det_features(DevTables t, const u64* alpha, const u64* beta, c
         e += ((b[w] >> (p - 1 - 64 * w)) & 1ull) ? hp : -hp;
       }
     }
-    out[k] = make_float4(0.5f * ra, 0.5f * rb, (float)e, (float)open);
+    out[k] = make_float4(0.5f * ra, 0.5f * rb, (float)e, 0.f);
+  }
+}
+
+// coupling strength of each row: log10(sum_J H_IJ^2) / 4 (the scale of the
+// second-order shift of the diagonal denominator), one warp per row, into .w
+__global__ void k_row_coupling(const int64_t* rowptr, const double* val, float4* out, int64_t N) {
+  const int lane = threadIdx.x & 31;
+  const int64_t warp = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
+  const int64_t nwarp = ((int64_t)gridDim.x * blockDim.x) >> 5;
+  for (int64_t k = warp; k < N; k += nwarp) {
+    double s = 0.0;
+    for (int64_t e = rowptr[k] + lane; e < rowptr[k + 1]; e += 32) s = fma(val[e], val[e], s);
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+    if (lane == 0) out[k].w = (float)(log10(s + 1e-30) * 0.25);
   }
 }
 
@@ -203,6 +218,7 @@ int qp_det_features(qpgpu_ctx* c) {
   else
     k_det_features<2><<<gsz(c->N), 256, 0, c->stream>>>(c->tab, c->d_alpha, c->d_beta, c->d_rows, c->d_cols,
                                                         (float4*)c->d_detfeat, c->N);
+  k_row_coupling<<<gsz(c->N * 32), 256, 0, c->stream>>>(c->d_rowptr, c->d_val64, (float4*)c->d_detfeat, c->N);
   QP_CUDA(c, cudaGetLastError());
   return 0;
 }

@@ -404,7 +404,7 @@ struct qpgpu_ctx {
   double setup_ms = 0.0;
   SigmaItems items;
   MlpState mlp;
-  float* d_detfeat = nullptr;  // (N, 4): alpha rank, beta rank, orbital-energy sum, open shells
+  float* d_detfeat = nullptr;  // (N, 4): alpha rank, beta rank, orbital-energy sum, log10(sum_J H_IJ^2)/4
   // optional phase timing of the set-up (environment QPGPU_PROFILE=1)
   bool profile = false;
   std::vector<std::pair<std::string, cudaEvent_t>> marks;
@@ -471,7 +471,7 @@ __device__ __forceinline__ void qp_features(const float4 st, double hmL, double 
   f[1] = st.y * 0.25f;
   f[2] = (float)(hmL * 0.1);
   f[3] = st.z * 0.1f;
-  f[4] = st.w * 0.125f;
+  f[4] = st.w;
   f[5] = (float)(log10(fabs(c) + 1e-30) / 8.0);
   f[6] = (float)(log10(fabs(r) + 1e-30) / 8.0);
   f[7] = (float)(log10(fabs(d) + 1e-30) / 8.0);
