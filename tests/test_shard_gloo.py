@@ -1,0 +1,91 @@
+"""Row-sharded sigma on two gloo ranks (CPU), with an injected rank failure.
+
+Each rank computes its row tasks with the CPU oracle's range sigma (the
+restatement of H_S2_u_0_nstates_openmp_work) and the ranks sum the results,
+as the reference's ZMQ collector does (davidson_parallel.irp.f:220-255).  The
+failure case makes rank 1 raise before the collective: rank 0 must report a
+ShardError instead of hanging.
+"""
+import datetime
+import os
+import socket
+import sys
+
+import numpy as np
+import pytest
+import torch.multiprocessing as mp
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def _port():
+    with socket.socket() as s:
+        s.bind(("127.0.0.1", 0))
+        return s.getsockname()[1]
+
+
+def _worker(rank, world, port, fail_rank, outdir):
+    sys.path.insert(0, ROOT)
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import torch.distributed as dist
+
+    from oracle import Oracle
+    from quantum_package_gb300 import generate as G
+    from quantum_package_gb300.shard import ShardError, sharded_sigma
+
+    os.environ["MASTER_ADDR"] = "127.0.0.1"
+    os.environ["MASTER_PORT"] = str(port)
+    dist.init_process_group("gloo", rank=rank, world_size=world, timeout=datetime.timedelta(seconds=10))
+    p = G.make_problem(1, n_det=3000)
+    o = Oracle.from_problem(p)
+    u_t = np.ascontiguousarray(G.random_coefficients(p.n_det, 2, 5).T)
+
+    def rows(u, i0, i1):
+        return o.h_s2_u0_work(u, i0, i1, 0, 1)
+
+    status = "ok"
+    try:
+        if rank == fail_rank:
+            raise RuntimeError("injected failure")
+        v, s = sharded_sigma(rows, u_t, rank, world, task_rows=700)
+        vf, sf = o.h_s2_u0_work(u_t, 1, p.n_det, 0, 1)
+        err = max(np.abs(v - vf).max(), np.abs(s - sf).max())
+        status = f"ok {err:.3e}"
+    except ShardError as e:
+        status = f"shard_error {e}"
+    except RuntimeError as e:
+        status = f"raised {e}"
+    with open(os.path.join(outdir, f"rank{rank}.txt"), "w") as f:
+        f.write(status)
+    if rank != fail_rank:
+        try:
+            dist.destroy_process_group()
+        except Exception:
+            pass
+
+
+def _run(world, fail_rank, tmp_path):
+    ctx = mp.get_context("spawn")
+    port = _port()
+    procs = [ctx.Process(target=_worker, args=(r, world, port, fail_rank, str(tmp_path))) for r in range(world)]
+    for p in procs:
+        p.start()
+    for p in procs:
+        p.join(timeout=120)
+        if p.is_alive():
+            p.kill()
+            pytest.fail("rank did not finish")
+    return [open(tmp_path / f"rank{r}.txt").read() for r in range(world)]
+
+
+def test_two_ranks_match_single_rank(tmp_path):
+    out = _run(2, -1, tmp_path)
+    for s in out:
+        assert s.startswith("ok"), s
+        assert float(s.split()[1]) < 1e-12
+
+
+def test_failed_rank_is_detected(tmp_path):
+    out = _run(2, 1, tmp_path)
+    assert out[1].startswith("raised injected failure")
+    assert out[0].startswith("shard_error"), out[0]
