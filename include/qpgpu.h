@@ -188,6 +188,36 @@ int qpgpu_mlp_gradient(qpgpu_ctx* ctx, const float* X, const float* g, const flo
 int qpgpu_mlp_predict(qpgpu_ctx* ctx, const float* X, int64_t n, float* y);
 int qpgpu_mlp_train(qpgpu_ctx* ctx, int epochs, int batch, float lr, uint64_t seed, float* loss);
 
+/* Batches of independent CI problems (no counterpart in the reference, which
+ * solves one problem per process).  A batch wraps contexts whose integrals
+ * and determinants are set; sigma for all problems is one persistent launch
+ * over a work queue of (problem, row chunk) items, the Davidson algebra of all
+ * problems runs in batched kernels, the device part of each iteration is
+ * replayed from CUDA graphs, and the persistent kernel's launch shape is
+ * autotuned on the first call.  All problems must share S_z. */
+typedef struct qpgpu_batch qpgpu_batch;
+typedef struct qpgpu_batch_stats {
+  int32_t n_iter;              /* Davidson iterations (all problems advance together) */
+  int32_t n_sigma_launches;    /* persistent sigma launches */
+  int32_t n_converged;         /* problems that met the threshold */
+  int32_t tuned_warps;         /* chosen warps per block of the persistent sigma */
+  int32_t tuned_blocks_per_sm; /* chosen resident blocks per SM */
+  int32_t pad;
+  double elapsed_ms;           /* device time of the iterations */
+  double tune_ms;              /* time spent by the autotuner (first call) */
+  int32_t* iters;              /* optional [n]: iterations of each problem */
+} qpgpu_batch_stats;
+int qpgpu_batch_create(qpgpu_ctx* const* ctxs, int n, qpgpu_batch** out);
+int qpgpu_batch_destroy(qpgpu_batch* batch);
+const char* qpgpu_batch_last_error(qpgpu_batch* batch);
+/* davidson_diag_hjj_sjj (diagonalization_hs2.irp.f:52-444) on every problem:
+ * u_in[p] host (dim_in[p], n_states_diag) guesses in psi_det order, replaced
+ * by the eigenvectors; energies and s2_out: n x n_states_diag (row p for
+ * problem p); n_states[p] <= params->n_states_diag; diagonal step only. */
+int qpgpu_batch_davidson(qpgpu_batch* batch, double* const* u_in, const int64_t* dim_in, const int* n_states,
+                         double* energies, double* s2_out, const qpgpu_davidson_params* params,
+                         qpgpu_batch_stats* stats);
+
 /* psi_bilinear_matrix_order (spindeterminants.irp.f:387-445), 0-based, host:
  * order[k] = psi_det index of bilinear position k. */
 int qpgpu_bilinear_order(qpgpu_ctx* ctx, int32_t* order);

@@ -48,6 +48,12 @@ class DavidsonTrace(C.Structure):
                 ("n_samples", C.c_int64)]
 
 
+class BatchStats(C.Structure):
+    _fields_ = [("n_iter", C.c_int32), ("n_sigma_launches", C.c_int32), ("n_converged", C.c_int32),
+                ("tuned_warps", C.c_int32), ("tuned_blocks_per_sm", C.c_int32), ("pad", C.c_int32),
+                ("elapsed_ms", C.c_double), ("tune_ms", C.c_double), ("iters", C.c_void_p)]
+
+
 MLP_NPARAM = 4801
 
 
@@ -82,6 +88,11 @@ def load():
         "qpgpu_sigma_bilinear": (C.c_int, [vp, vp, vp, vp, vp, C.c_int, C.c_int, vp]),
         "qpgpu_sigma_bilinear_noalloc": (C.c_int, [vp, vp, vp, vp, vp, C.c_int, C.c_int, vp]),
         "qpgpu_bilinear_order": (C.c_int, [vp, vp]),
+        "qpgpu_batch_create": (C.c_int, [vp, C.c_int, C.POINTER(vp)]),
+        "qpgpu_batch_destroy": (C.c_int, [vp]),
+        "qpgpu_batch_last_error": (C.c_char_p, [vp]),
+        "qpgpu_batch_davidson": (C.c_int, [vp, vp, vp, vp, vp, vp, C.POINTER(DavidsonParams),
+                                           C.POINTER(BatchStats)]),
         "qpgpu_mlp_init": (C.c_int, [vp, C.c_uint64]),
         "qpgpu_mlp_set_weights": (C.c_int, [vp, vp]),
         "qpgpu_mlp_get_weights": (C.c_int, [vp, vp]),

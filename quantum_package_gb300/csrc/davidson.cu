@@ -27,6 +27,61 @@
 
 #include "qpgpu_internal.cuh"
 
+// Host cyclic Jacobi eigen-solver for the small projected matrix (stands in
+// for lapack_diag/dsyev, LinearAlgebra.irp.f:446-512): eigenvalues ascending,
+// eigenvectors in the columns of v (n x n, row-major v[i*n+j] = component i of
+// vector j).
+void qp_jacobi(std::vector<double> a, int n, std::vector<double>& w, std::vector<double>& v) {
+  v.assign((size_t)n * n, 0.0);
+  for (int i = 0; i < n; ++i) v[(size_t)i * n + i] = 1.0;
+  for (int sweep = 0; sweep < 64; ++sweep) {
+    double off = 0.0, tot = 0.0;
+    for (int i = 0; i < n; ++i)
+      for (int j = 0; j < n; ++j) {
+        const double x = a[(size_t)i * n + j] * a[(size_t)i * n + j];
+        tot += x;
+        if (i != j) off += x;
+      }
+    if (off == 0.0 || off <= 1e-32 * tot) break;
+    for (int p = 0; p < n - 1; ++p)
+      for (int q = p + 1; q < n; ++q) {
+        const double apq = a[(size_t)p * n + q];
+        if (apq == 0.0) continue;
+        const double app = a[(size_t)p * n + p], aqq = a[(size_t)q * n + q];
+        const double theta = (aqq - app) / (2.0 * apq);
+        const double t = (theta >= 0 ? 1.0 : -1.0) / (std::fabs(theta) + std::sqrt(theta * theta + 1.0));
+        const double c = 1.0 / std::sqrt(t * t + 1.0), s = t * c;
+        for (int k = 0; k < n; ++k) {  // columns p, q
+          const double akp = a[(size_t)k * n + p], akq = a[(size_t)k * n + q];
+          a[(size_t)k * n + p] = c * akp - s * akq;
+          a[(size_t)k * n + q] = s * akp + c * akq;
+        }
+        for (int k = 0; k < n; ++k) {  // rows p, q
+          const double apk = a[(size_t)p * n + k], aqk = a[(size_t)q * n + k];
+          a[(size_t)p * n + k] = c * apk - s * aqk;
+          a[(size_t)q * n + k] = s * apk + c * aqk;
+        }
+        for (int k = 0; k < n; ++k) {
+          const double vkp = v[(size_t)k * n + p], vkq = v[(size_t)k * n + q];
+          v[(size_t)k * n + p] = c * vkp - s * vkq;
+          v[(size_t)k * n + q] = s * vkp + c * vkq;
+        }
+      }
+  }
+  std::vector<int> ord(n);
+  std::iota(ord.begin(), ord.end(), 0);
+  std::stable_sort(ord.begin(), ord.end(),
+                   [&](int x, int y) { return a[(size_t)x * n + x] < a[(size_t)y * n + y]; });
+  std::vector<double> v2((size_t)n * n);
+  w.resize(n);
+  for (int j = 0; j < n; ++j) {
+    w[j] = a[(size_t)ord[j] * n + ord[j]];
+    for (int i = 0; i < n; ++i) v2[(size_t)i * n + j] = v[(size_t)i * n + ord[j]];
+  }
+  v.swap(v2);
+}
+
+
 namespace {
 
 constexpr int DBLK = 256;
@@ -422,60 +477,6 @@ __global__ void k_copy(const double* a, double* b, int64_t n) {
     b[i] = a[i];
 }
 
-// Host cyclic Jacobi eigen-solver for the small projected matrix (stands in
-// for lapack_diag/dsyev, LinearAlgebra.irp.f:446-512): eigenvalues ascending,
-// eigenvectors in the columns of v (n x n, row-major v[i*n+j] = component i of
-// vector j).
-void jacobi(std::vector<double> a, int n, std::vector<double>& w, std::vector<double>& v) {
-  v.assign((size_t)n * n, 0.0);
-  for (int i = 0; i < n; ++i) v[(size_t)i * n + i] = 1.0;
-  for (int sweep = 0; sweep < 64; ++sweep) {
-    double off = 0.0, tot = 0.0;
-    for (int i = 0; i < n; ++i)
-      for (int j = 0; j < n; ++j) {
-        const double x = a[(size_t)i * n + j] * a[(size_t)i * n + j];
-        tot += x;
-        if (i != j) off += x;
-      }
-    if (off == 0.0 || off <= 1e-32 * tot) break;
-    for (int p = 0; p < n - 1; ++p)
-      for (int q = p + 1; q < n; ++q) {
-        const double apq = a[(size_t)p * n + q];
-        if (apq == 0.0) continue;
-        const double app = a[(size_t)p * n + p], aqq = a[(size_t)q * n + q];
-        const double theta = (aqq - app) / (2.0 * apq);
-        const double t = (theta >= 0 ? 1.0 : -1.0) / (std::fabs(theta) + std::sqrt(theta * theta + 1.0));
-        const double c = 1.0 / std::sqrt(t * t + 1.0), s = t * c;
-        for (int k = 0; k < n; ++k) {  // columns p, q
-          const double akp = a[(size_t)k * n + p], akq = a[(size_t)k * n + q];
-          a[(size_t)k * n + p] = c * akp - s * akq;
-          a[(size_t)k * n + q] = s * akp + c * akq;
-        }
-        for (int k = 0; k < n; ++k) {  // rows p, q
-          const double apk = a[(size_t)p * n + k], aqk = a[(size_t)q * n + k];
-          a[(size_t)p * n + k] = c * apk - s * aqk;
-          a[(size_t)q * n + k] = s * apk + c * aqk;
-        }
-        for (int k = 0; k < n; ++k) {
-          const double vkp = v[(size_t)k * n + p], vkq = v[(size_t)k * n + q];
-          v[(size_t)k * n + p] = c * vkp - s * vkq;
-          v[(size_t)k * n + q] = s * vkp + c * vkq;
-        }
-      }
-  }
-  std::vector<int> ord(n);
-  std::iota(ord.begin(), ord.end(), 0);
-  std::stable_sort(ord.begin(), ord.end(),
-                   [&](int x, int y) { return a[(size_t)x * n + x] < a[(size_t)y * n + y]; });
-  std::vector<double> v2((size_t)n * n);
-  w.resize(n);
-  for (int j = 0; j < n; ++j) {
-    w[j] = a[(size_t)ord[j] * n + ord[j]];
-    for (int i = 0; i < n; ++i) v2[(size_t)i * n + j] = v[(size_t)i * n + ord[j]];
-  }
-  v.swap(v2);
-}
-
 struct Dav {
   qpgpu_ctx* c;
   cudaStream_t st;
@@ -699,7 +700,7 @@ extern "C" int qpgpu_davidson_hs2(qpgpu_ctx* c, double* u_in, int64_t dim_in, do
           hs[(size_t)i * shift2 + j] = h[(size_t)i * mmax + j];
           ss[(size_t)i * shift2 + j] = s_[(size_t)i * mmax + j];
         }
-      jacobi(hs, shift2, wv, y);
+      qp_jacobi(hs, shift2, wv, y);
       for (int k = 0; k < shift2; ++k) lambda[k] = wv[k];
       // S^2 of the Ritz vectors (:289-301): s2_k = y_k^T s y_k + S_z(S_z-1)
       for (int k = 0; k < shift2; ++k) {

@@ -496,3 +496,7 @@ __device__ __forceinline__ float qp_mlp_forward(const float* P, const float* f) 
   return y;
 }
 #endif
+
+// small symmetric eigenproblem on the host (davidson.cu): ascending
+// eigenvalues, eigenvectors in the columns of v (row-major n x n)
+void qp_jacobi(std::vector<double> a, int n, std::vector<double>& w, std::vector<double>& v);

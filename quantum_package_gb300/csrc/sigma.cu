@@ -9,6 +9,7 @@
 // as u_t(N_st, N_det) in the reference (:27-41), so the N_st coefficients of a
 // connected determinant J are one contiguous load.
 #include "qpgpu_internal.cuh"
+#include "sigma_device.cuh"
 
 namespace {
 
@@ -44,121 +45,7 @@ __device__ __forceinline__ bool row_selected(const SigArgs& a, int k) {
   return ((k - a.row_first) % a.row_step) == 0;
 }
 
-// ---- cross-lane reductions ---------------------------------------------
-// Reduce-scatter of NSTP per-lane partial sums over the 32 lanes of a warp:
-// each round halves the values a lane keeps (exchanging the other half with
-// its partner), then plain butterflies finish.  A lane performs
-// log2(NSTP) + ... = 5 + NSTP - 1 - log2(NSTP) additions instead of 5 * NSTP,
-// which matters on GB300 where FP64 issue is scarce.  On return acc[0] of lane
-// L holds the full sum of state (L >> (5 - log2 NSTP)).  The order of the
-// additions is fixed, so results are deterministic.
-template <int NSTP>
-__device__ __forceinline__ double reduce_scatter64(double (&acc)[NSTP], int lane) {
-  int off = 16;
-#pragma unroll
-  for (int m = NSTP; m > 1; m >>= 1, off >>= 1) {
-    const bool up = lane & off;
-#pragma unroll
-    for (int i = 0; i < m / 2; ++i) {
-      const double send = up ? acc[i] : acc[i + m / 2];
-      const double keep = up ? acc[i + m / 2] : acc[i];
-      acc[i] = keep + __shfl_xor_sync(0xffffffffu, send, off);
-    }
-  }
-  double x = acc[0];
-#pragma unroll
-  for (; off > 0; off >>= 1) x += __shfl_xor_sync(0xffffffffu, x, off);
-  return x;
-}
-
-// error-free sum of two floats (Knuth TwoSum)
-__device__ __forceinline__ void two_sum(float a, float b, float& s, float& e) {
-  s = __fadd_rn(a, b);
-  const float bb = __fsub_rn(s, a);
-  e = __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(b, bb));
-}
-
-// float-float (hi, lo) version of reduce_scatter64, all arithmetic in FP32
-template <int NSTP>
-__device__ __forceinline__ void reduce_scatter_ff(float (&hi)[NSTP], float (&lo)[NSTP], int lane, float& rh,
-                                                  float& rl) {
-  int off = 16;
-#pragma unroll
-  for (int m = NSTP; m > 1; m >>= 1, off >>= 1) {
-    const bool up = lane & off;
-#pragma unroll
-    for (int i = 0; i < m / 2; ++i) {
-      const float sh = up ? hi[i] : hi[i + m / 2], sl = up ? lo[i] : lo[i + m / 2];
-      const float kh = up ? hi[i + m / 2] : hi[i], kl = up ? lo[i + m / 2] : lo[i];
-      const float oh = __shfl_xor_sync(0xffffffffu, sh, off), ol = __shfl_xor_sync(0xffffffffu, sl, off);
-      float s, e;
-      two_sum(kh, oh, s, e);
-      const float l = __fadd_rn(__fadd_rn(kl, ol), e);
-      hi[i] = __fadd_rn(s, l);
-      lo[i] = __fsub_rn(l, __fsub_rn(hi[i], s));
-    }
-  }
-  float h = hi[0], l = lo[0];
-#pragma unroll
-  for (; off > 0; off >>= 1) {
-    const float oh = __shfl_xor_sync(0xffffffffu, h, off), ol = __shfl_xor_sync(0xffffffffu, l, off);
-    float s, e;
-    two_sum(h, oh, s, e);
-    const float t = __fadd_rn(__fadd_rn(l, ol), e);
-    h = __fadd_rn(s, t);
-    l = __fsub_rn(t, __fsub_rn(h, s));
-  }
-  rh = h;
-  rl = l;
-}
-
-template <int NST>
-struct Pow2 {
-  static constexpr int v = NST <= 1 ? 1 : NST <= 2 ? 2 : NST <= 4 ? 4 : 8;
-  static constexpr int lg = NST <= 1 ? 0 : NST <= 2 ? 1 : NST <= 4 ? 2 : 3;
-};
-
-// coefficient row of determinant `col`: vector loads where the layout allows
-template <int NST>
-__device__ __forceinline__ void load_row(const double* u, int64_t col, double (&x)[NST]) {
-  const double* p = u + col * NST;
-  if constexpr (NST % 2 == 0) {
-#pragma unroll
-    for (int i = 0; i < NST; i += 2) {
-      const double2 t = __ldg(reinterpret_cast<const double2*>(p + i));
-      x[i] = t.x;
-      x[i + 1] = t.y;
-    }
-  } else {
-#pragma unroll
-    for (int i = 0; i < NST; ++i) x[i] = __ldg(p + i);
-  }
-}
-
-template <int NST>
-__device__ __forceinline__ void load_row(const float* u, int64_t col, float (&x)[NST]) {
-  const float* p = u + col * NST;
-  if constexpr (NST % 4 == 0) {
-#pragma unroll
-    for (int i = 0; i < NST; i += 4) {
-      const float4 t = __ldg(reinterpret_cast<const float4*>(p + i));
-      x[i] = t.x;
-      x[i + 1] = t.y;
-      x[i + 2] = t.z;
-      x[i + 3] = t.w;
-    }
-  } else if constexpr (NST % 2 == 0) {
-#pragma unroll
-    for (int i = 0; i < NST; i += 2) {
-      const float2 t = __ldg(reinterpret_cast<const float2*>(p + i));
-      x[i] = t.x;
-      x[i + 1] = t.y;
-    }
-  } else {
-#pragma unroll
-    for (int i = 0; i < NST; ++i) x[i] = __ldg(p + i);
-  }
-}
+using namespace qpsig;
 
 // write the reduced state sums (lane L holds state L >> shift) and the diagonal
 template <int NST>
@@ -177,6 +64,8 @@ __device__ __forceinline__ void store_row(const SigArgs& a, int64_t it, int k, i
     a.ps[it * NST + st] = has_s2 ? sv : 0.0;
   }
 }
+
+
 
 constexpr int UNR = 2;  // pairs per lane per loop trip (independent loads in flight)
 
