@@ -53,6 +53,7 @@ def parse():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-davidson", action="store_true", help="skip the Davidson time-to-E block")
     ap.add_argument("--davidson-only", action="store_true", help="only the Davidson block (profiling)")
+    ap.add_argument("--n-states-diag", type=int, default=6, help="N_st_diag of the Davidson runs")
     return ap.parse_args()
 
 
@@ -265,6 +266,8 @@ def davidson_block(prob, wf):
 
 
 def run_ours(args):
+    global N_STATES_DIAG
+    N_STATES_DIAG = args.n_states_diag
     import torch
     rank, world, local = dist_env()
     torch.cuda.set_device(local)

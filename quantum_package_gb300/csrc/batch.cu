@@ -132,17 +132,27 @@ __global__ void k_bsigma(const BProb* __restrict__ probs, int np, int64_t total,
       float sum[NP], cmp[NP];
 #pragma unroll
       for (int st = 0; st < NP; ++st) sum[st] = cmp[st] = 0.f;
-      for (int64_t e = beg + lane; e < end; e += 32) {
-        const int col = __ldg(&P.colidx[e]);
-        const float hv = __ldg(&P.val32[e]);
-        float x[NST];
-        load_row<NST>(u32, col, x);
+      constexpr int U4 = 4;  // independent loads in flight per lane
+      for (int64_t e0 = beg + lane; e0 < end; e0 += 32 * U4) {
+        int col[U4];
+        float hv[U4];
 #pragma unroll
-        for (int st = 0; st < NST; ++st) {
-          const float y = __fmaf_rn(hv, x[st], -cmp[st]);
-          const float t = __fadd_rn(sum[st], y);
-          cmp[st] = __fsub_rn(__fsub_rn(t, sum[st]), y);
-          sum[st] = t;
+        for (int q = 0; q < U4; ++q) {
+          const int64_t e = e0 + 32 * q;
+          col[q] = e < end ? __ldg(&P.colidx[e]) : k;
+          hv[q] = e < end ? __ldg(&P.val32[e]) : 0.f;
+        }
+#pragma unroll
+        for (int q = 0; q < U4; ++q) {
+          float x[NST];
+          load_row<NST>(u32, col[q], x);
+#pragma unroll
+          for (int st = 0; st < NST; ++st) {
+            const float y = __fmaf_rn(hv[q], x[st], -cmp[st]);
+            const float t = __fadd_rn(sum[st], y);
+            cmp[st] = __fsub_rn(__fsub_rn(t, sum[st]), y);
+            sum[st] = t;
+          }
         }
       }
 #pragma unroll
@@ -154,13 +164,23 @@ __global__ void k_bsigma(const BProb* __restrict__ probs, int np, int64_t total,
       double acc[NP];
 #pragma unroll
       for (int st = 0; st < NP; ++st) acc[st] = 0.0;
-      for (int64_t e = beg + lane; e < end; e += 32) {
-        const int col = __ldg(&P.colidx[e]);
-        const double hv = __ldg(&P.val64[e]);
-        double x[NST];
-        load_row<NST>(u, col, x);
+      constexpr int U2 = 2;
+      for (int64_t e0 = beg + lane; e0 < end; e0 += 32 * U2) {
+        int col[U2];
+        double hv[U2];
 #pragma unroll
-        for (int st = 0; st < NST; ++st) acc[st] = fma(hv, x[st], acc[st]);
+        for (int q = 0; q < U2; ++q) {
+          const int64_t e = e0 + 32 * q;
+          col[q] = e < end ? __ldg(&P.colidx[e]) : k;
+          hv[q] = e < end ? __ldg(&P.val64[e]) : 0.0;
+        }
+#pragma unroll
+        for (int q = 0; q < U2; ++q) {
+          double x[NST];
+          load_row<NST>(u, col[q], x);
+#pragma unroll
+          for (int st = 0; st < NST; ++st) acc[st] = fma(hv[q], x[st], acc[st]);
+        }
       }
       hsum = reduce_scatter64<NP>(acc, lane);
     }

@@ -67,7 +67,8 @@ __device__ __forceinline__ void store_row(const SigArgs& a, int64_t it, int k, i
 
 
 
-constexpr int UNR = 2;  // pairs per lane per loop trip (independent loads in flight)
+constexpr int UNR = 2;    // FP64 sigma: pairs per lane per loop trip (FP64-pipe bound)
+constexpr int UNR32 = 4;  // FP32 sigma: more independent loads in flight (latency bound)
 
 template <int NST>
 __global__ void __launch_bounds__(SBLK) k_sigma64(SigArgs a) {
@@ -142,17 +143,17 @@ __global__ void __launch_bounds__(SBLK) k_sigma32(SigArgs a) {
     float sum[NP], cmp[NP];
 #pragma unroll
     for (int st = 0; st < NP; ++st) sum[st] = cmp[st] = 0.f;
-    for (int64_t e0 = beg + lane; e0 < end; e0 += 32 * UNR) {
-      int col[UNR];
-      float hv[UNR];
+    for (int64_t e0 = beg + lane; e0 < end; e0 += 32 * UNR32) {
+      int col[UNR32];
+      float hv[UNR32];
 #pragma unroll
-      for (int q = 0; q < UNR; ++q) {
+      for (int q = 0; q < UNR32; ++q) {
         const int64_t e = e0 + 32 * q;
         col[q] = e < end ? __ldg(&a.colidx[e]) : k;
         hv[q] = e < end ? __ldg(&a.val32[e]) : 0.f;
       }
 #pragma unroll
-      for (int q = 0; q < UNR; ++q) {
+      for (int q = 0; q < UNR32; ++q) {
         float x[NST];
         load_row<NST>(a.u32, col[q], x);
 #pragma unroll
