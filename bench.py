@@ -48,8 +48,10 @@ def parse():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--n-det", type=int, default=1_000_000)
-    ap.add_argument("--cpu-sample-step", type=int, default=250,
-                    help="row stride of the CPU-oracle sample (1/step of the rows)")
+    ap.add_argument("--cpu-sample-step", type=int, default=10,
+                    help="row stride of the CPU-oracle sample (1/step of the rows, about 10-15 s on 16 cores)")
+    ap.add_argument("--reference-budget-s", type=float, default=150.0,
+                    help="wall-time budget of the whole --impl reference run (warm-up + timed steps)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-davidson", action="store_true", help="skip the Davidson time-to-E block")
     ap.add_argument("--davidson-only", action="store_true", help="only the Davidson block (profiling)")
@@ -165,7 +167,13 @@ def run_reference(args):
     from oracle import Oracle, num_threads
     o = Oracle.from_problem(prob)
     u_t = np.ascontiguousarray(G.random_coefficients(prob.n_det, N_STATES, prob.seed).T)
-    step = args.cpu_sample_step
+    # per-step sample: a row stride sized so that warm-up + timed steps fit the
+    # budget (calibrated on a 1/1000 sample), never denser than --cpu-sample-step
+    t = time.perf_counter()
+    o.h_s2_u0_work(u_t, 1, prob.n_det, 0, 1000)
+    rows_per_s = len(range(0, prob.n_det, 1000)) / max(time.perf_counter() - t, 1e-6)
+    per_step_s = args.reference_budget_s / max(1, args.steps + args.warmup)
+    step = max(args.cpu_sample_step, int(np.ceil(prob.n_det / max(1.0, rows_per_s * per_step_s))))
     rows = len(range(0, prob.n_det, step))
     for _ in range(args.warmup):
         o.h_s2_u0_work(u_t, 1, prob.n_det, 0, step)

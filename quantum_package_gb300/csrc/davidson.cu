@@ -570,6 +570,43 @@ void orthonormalise(Dav& d, int b) {
   }
 }
 
+// Per-phase stream timeline of one Davidson run (environment QPGPU_PROFILE=1):
+// an event closes each phase, and the time between consecutive events is
+// charged to the phase that ended, so host work between launches (the small
+// eigenproblem) shows up as the gap it leaves on the stream.
+struct DavProf {
+  enum { OTHER, ORTHO, SIGMA, GRAM, HOST, RITZ, STEP, RESTART, NPH };
+  bool on = false;
+  cudaStream_t st = nullptr;
+  std::vector<std::pair<int, cudaEvent_t>> ev;
+  void mark(int phase) {
+    if (!on) return;
+    cudaEvent_t e;
+    if (cudaEventCreate(&e) != cudaSuccess) return;
+    cudaEventRecord(e, st);
+    ev.emplace_back(phase, e);
+  }
+  void report(int n_sigma) {
+    if (!on || ev.size() < 2) return;
+    static const char* names[NPH] = {"other", "orthonormalise", "sigma", "gram W,S", "host small eig",
+                                     "ritz vectors", "step + norms", "restart"};
+    double ms[NPH] = {0};
+    cudaEventSynchronize(ev.back().second);
+    for (size_t i = 1; i < ev.size(); ++i) {
+      float t = 0.f;
+      cudaEventElapsedTime(&t, ev[i - 1].second, ev[i].second);
+      ms[ev[i].first] += t;
+    }
+    double tot = 0;
+    for (double x : ms) tot += x;
+    for (int p = 0; p < NPH; ++p)
+      fprintf(stderr, "[qpgpu davidson] %-16s %10.3f ms  %5.1f%%  %8.3f ms/sigma\n", names[p], ms[p],
+              100.0 * ms[p] / tot, ms[p] / std::max(1, n_sigma));
+    for (auto& e : ev) cudaEventDestroy(e.second);
+    ev.clear();
+  }
+};
+
 }  // namespace
 
 extern "C" int qpgpu_davidson_hs2(qpgpu_ctx* c, double* u_in, int64_t dim_in, double* energies, double* s2_out,
@@ -666,12 +703,17 @@ extern "C" int qpgpu_davidson_hs2(qpgpu_ctx* c, double* u_in, int64_t dim_in, do
     }
     ++trace_n;
   };
+  DavProf prof;
+  prof.on = c->profile;
+  prof.st = st;
+  prof.mark(DavProf::OTHER);
   while (!converged && !failed && n_sigma < max_sigma) {
     for (int iter = 1; iter <= itermax - 1; ++iter) {
       const int b = iter - 1;
       const int shift = nsd * b;
       shift2 = nsd * iter;
       orthonormalise(d, b);
+      prof.mark(DavProf::ORTHO);
       // sigma on block b
       const int prec = (mixed && iter > 1) ? QPGPU_FP32 : QPGPU_FP64;
       if (prec == QPGPU_FP32) qp_to_float(d.blk(d.U, b), d.u32, (int64_t)blkn, st);
@@ -679,6 +721,7 @@ extern "C" int qpgpu_davidson_hs2(qpgpu_ctx* c, double* u_in, int64_t dim_in, do
                                (int)N, 0, 1);
       if (rc) return rc;
       ++n_sigma;
+      prof.mark(DavProf::SIGMA);
       // new Gram columns
       gram(d, d.U, shift2, d.blk(d.W, b), d.small);
       gram(d, d.U, shift2, d.blk(d.S, b), d.small + MAXM * MAXS);
@@ -686,6 +729,7 @@ extern "C" int qpgpu_davidson_hs2(qpgpu_ctx* c, double* u_in, int64_t dim_in, do
       QP_CUDA(c, cudaMemcpyAsync(scol.data(), d.small + MAXM * MAXS, (size_t)shift2 * nsd * sizeof(double),
                                  cudaMemcpyDeviceToHost, st));
       QP_CUDA(c, cudaStreamSynchronize(st));
+      prof.mark(DavProf::GRAM);
       for (int i = 0; i < shift2; ++i)
         for (int j = 0; j < nsd; ++j) {
           const int col = shift + j;
@@ -733,8 +777,10 @@ extern "C" int qpgpu_davidson_hs2(qpgpu_ctx* c, double* u_in, int64_t dim_in, do
       for (int i = 0; i < shift2; ++i)
         for (int j = 0; j < nsd; ++j) ycoef[(size_t)i * nsd + j] = y[(size_t)i * shift2 + j];
       double* ydev = d.small + 3 * MAXM * MAXS;
+      prof.mark(DavProf::HOST);
       QP_CUDA(c, cudaMemcpyAsync(ydev, ycoef.data(), ycoef.size() * sizeof(double), cudaMemcpyHostToDevice, st));
       lincomb(d, shift2, ydev, 0, d.U, d.blk(d.U, iter), d.W, d.blk(d.W, iter), d.S, d.blk(d.S, iter));
+      prof.mark(DavProf::RITZ);
       // Davidson step and residual norms (:386-395)
       StepParams sp{};
       for (int k = 0; k < nsd; ++k) {
@@ -761,6 +807,7 @@ extern "C" int qpgpu_davidson_hs2(qpgpu_ctx* c, double* u_in, int64_t dim_in, do
       QP_CUDA(c, cudaGetLastError());
       QP_CUDA(c, cudaMemcpyAsync(partial.data(), d.part, partial.size() * sizeof(double), cudaMemcpyDeviceToHost, st));
       QP_CUDA(c, cudaStreamSynchronize(st));
+      prof.mark(DavProf::STEP);
       double mx = 0.0;
       for (int k = 0; k < nst; ++k) {
         double r = 0.0;
@@ -803,10 +850,12 @@ extern "C" int qpgpu_davidson_hs2(qpgpu_ctx* c, double* u_in, int64_t dim_in, do
     QP_CUDA(c, cudaMemcpyAsync(ydev, ycoef.data(), ycoef.size() * sizeof(double), cudaMemcpyHostToDevice, st));
     lincomb(d, shift2, ydev, 0, d.U, d.R);
     k_copy<<<gsz((int64_t)blkn), DBLK, 0, st>>>(d.R, d.U, (int64_t)blkn);
+    prof.mark(DavProf::RESTART);
     for (int i = 0; i < mmax; ++i)
       for (int j = 0; j < mmax; ++j) h[(size_t)i * mmax + j] = s_[(size_t)i * mmax + j] = 0.0;
   }
   QP_CUDA(c, cudaGetLastError());
+  prof.report(n_sigma);
   // training pairs from the captured iterations, with the final vectors
   if (n_cap > 0 && !failed) {
     const int nslot = n_cap * nst;
