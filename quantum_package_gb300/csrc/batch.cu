@@ -861,7 +861,7 @@ int qpgpu_batch_davidson(qpgpu_batch* B, double* const* u_in, const int64_t* dim
             hs[(size_t)i * shift2 + j] = h[(size_t)i * mmax + j];
             ss[(size_t)i * shift2 + j] = s[(size_t)i * mmax + j];
           }
-        qp_jacobi(hs, shift2, w, y);
+        qp_eigh(hs, shift2, w, y);
         for (int k = 0; k < shift2; ++k) {
           double acc = 0.0;
           for (int i = 0; i < shift2; ++i) {

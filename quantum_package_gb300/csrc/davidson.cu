@@ -23,64 +23,132 @@
 #include <algorithm>
 #include <cmath>
 #include <cstring>
+#include <limits>
 #include <numeric>
 
 #include "qpgpu_internal.cuh"
+#include "sigma_device.cuh"
 
-// Host cyclic Jacobi eigen-solver for the small projected matrix (stands in
-// for lapack_diag/dsyev, LinearAlgebra.irp.f:446-512): eigenvalues ascending,
+// Host eigen-solver for the small projected matrix (stands in for
+// lapack_diag/dsyev, LinearAlgebra.irp.f:446-512): eigenvalues ascending,
 // eigenvectors in the columns of v (n x n, row-major v[i*n+j] = component i of
-// vector j).
-void qp_jacobi(std::vector<double> a, int n, std::vector<double>& w, std::vector<double>& v) {
+// vector j).  Householder reduction to tridiagonal form with the reflections
+// accumulated, then the implicit QL iteration with a Wilkinson-type shift on
+// the tridiagonal matrix (Bowdler, Martin, Reinsch and Wilkinson, Numer. Math.
+// 11 (1968) 293; Golub and Van Loan, Matrix Computations, sec. 8.3): about
+// 9 n^3 flops with a fixed iteration count, where a cyclic Jacobi sweep costs
+// about 4 n^3 and needs several sweeps.
+void qp_eigh(std::vector<double> a, int n, std::vector<double>& w, std::vector<double>& v) {
+  w.assign(n, 0.0);
   v.assign((size_t)n * n, 0.0);
-  for (int i = 0; i < n; ++i) v[(size_t)i * n + i] = 1.0;
-  for (int sweep = 0; sweep < 64; ++sweep) {
-    double off = 0.0, tot = 0.0;
-    for (int i = 0; i < n; ++i)
-      for (int j = 0; j < n; ++j) {
-        const double x = a[(size_t)i * n + j] * a[(size_t)i * n + j];
-        tot += x;
-        if (i != j) off += x;
+  if (n <= 0) return;
+  // z holds the eigenvectors as rows (z[j*n+i] = component i of vector j), so
+  // that every update below runs along contiguous rows
+  std::vector<double> z((size_t)n * n, 0.0), x(n), p(n), q(n), t(n), e(n, 0.0);
+  for (int i = 0; i < n; ++i) z[(size_t)i * n + i] = 1.0;
+  // A <- H_k A H_k zeroes column k below the sub-diagonal; Z <- H_k Z
+  for (int k = 0; k + 2 < n; ++k) {
+    const int m = n - k - 1;  // length of the reflected part (rows k+1..n-1)
+    double nrm2 = 0.0;
+    for (int i = 0; i < m; ++i) {
+      x[i] = a[(size_t)(k + 1 + i) * n + k];
+      nrm2 += x[i] * x[i];
+    }
+    const double off2 = nrm2 - x[0] * x[0];
+    if (off2 == 0.0) continue;  // already tridiagonal in this column
+    double alpha = std::sqrt(nrm2);
+    if (x[0] > 0) alpha = -alpha;  // x - alpha e1 without cancellation
+    x[0] -= alpha;
+    const double beta = 2.0 / (x[0] * x[0] + off2);
+    // p = beta A_sub x, K = beta/2 p.x, q = p - K x, A_sub -= x q^T + q x^T
+    double px = 0.0;
+    for (int i = 0; i < m; ++i) {
+      const double* row = &a[(size_t)(k + 1 + i) * n + k + 1];
+      double s = 0.0;
+      for (int j = 0; j < m; ++j) s += row[j] * x[j];
+      p[i] = beta * s;
+      px += p[i] * x[i];
+    }
+    const double K = 0.5 * beta * px;
+    for (int i = 0; i < m; ++i) q[i] = p[i] - K * x[i];
+    for (int i = 0; i < m; ++i) {
+      double* row = &a[(size_t)(k + 1 + i) * n + k + 1];
+      const double xi = x[i], qi = q[i];
+      for (int j = 0; j < m; ++j) row[j] -= xi * q[j] + qi * x[j];
+    }
+    a[(size_t)(k + 1) * n + k] = a[(size_t)k * n + k + 1] = alpha;
+    for (int i = 1; i < m; ++i) a[(size_t)(k + 1 + i) * n + k] = a[(size_t)k * n + k + 1 + i] = 0.0;
+    // rows k+1.. of Z: Z_sub -= beta x (x^T Z_sub)
+    for (int c = 0; c < n; ++c) t[c] = 0.0;
+    for (int j = 0; j < m; ++j) {
+      const double* row = &z[(size_t)(k + 1 + j) * n];
+      const double xj = x[j];
+      for (int c = 0; c < n; ++c) t[c] += xj * row[c];
+    }
+    for (int j = 0; j < m; ++j) {
+      double* row = &z[(size_t)(k + 1 + j) * n];
+      const double bx = beta * x[j];
+      for (int c = 0; c < n; ++c) row[c] -= bx * t[c];
+    }
+  }
+  for (int i = 0; i < n; ++i) w[i] = a[(size_t)i * n + i];
+  for (int i = 0; i + 1 < n; ++i) e[i] = a[(size_t)(i + 1) * n + i];
+  e[n - 1] = 0.0;
+  // implicit QL on (w, e); each plane rotation mixes two rows of Z
+  const double eps = std::numeric_limits<double>::epsilon();
+  for (int l = 0; l < n; ++l) {
+    for (int iter = 0; iter < 64; ++iter) {
+      int m = l;
+      for (; m + 1 < n; ++m)
+        if (std::fabs(e[m]) <= eps * (std::fabs(w[m]) + std::fabs(w[m + 1]))) break;
+      if (m == l) break;
+      double g = (w[l + 1] - w[l]) / (2.0 * e[l]);
+      double r = std::fabs(g) < 1e150 ? std::sqrt(g * g + 1.0) : std::fabs(g);
+      g = w[m] - w[l] + e[l] / (g + (g >= 0 ? r : -r));
+      double sn = 1.0, cs = 1.0, shift = 0.0;
+      bool split = false;
+      for (int i = m - 1; i >= l; --i) {
+        const double f = sn * e[i], b = cs * e[i];
+        r = std::sqrt(f * f + g * g);
+        e[i + 1] = r;
+        if (r == 0.0) {  // the matrix splits at i: deflate and restart the sweep
+          w[i + 1] -= shift;
+          e[m] = 0.0;
+          split = true;
+          break;
+        }
+        sn = f / r;
+        cs = g / r;
+        g = w[i + 1] - shift;
+        r = (w[i] - g) * sn + 2.0 * cs * b;
+        shift = sn * r;
+        w[i + 1] = g + shift;
+        g = cs * r - b;
+        double* zi = &z[(size_t)i * n];
+        double* zj = &z[(size_t)(i + 1) * n];
+        for (int c = 0; c < n; ++c) {
+          const double u0 = zi[c], u1 = zj[c];
+          zj[c] = sn * u0 + cs * u1;
+          zi[c] = cs * u0 - sn * u1;
+        }
       }
-    if (off == 0.0 || off <= 1e-32 * tot) break;
-    for (int p = 0; p < n - 1; ++p)
-      for (int q = p + 1; q < n; ++q) {
-        const double apq = a[(size_t)p * n + q];
-        if (apq == 0.0) continue;
-        const double app = a[(size_t)p * n + p], aqq = a[(size_t)q * n + q];
-        const double theta = (aqq - app) / (2.0 * apq);
-        const double t = (theta >= 0 ? 1.0 : -1.0) / (std::fabs(theta) + std::sqrt(theta * theta + 1.0));
-        const double c = 1.0 / std::sqrt(t * t + 1.0), s = t * c;
-        for (int k = 0; k < n; ++k) {  // columns p, q
-          const double akp = a[(size_t)k * n + p], akq = a[(size_t)k * n + q];
-          a[(size_t)k * n + p] = c * akp - s * akq;
-          a[(size_t)k * n + q] = s * akp + c * akq;
-        }
-        for (int k = 0; k < n; ++k) {  // rows p, q
-          const double apk = a[(size_t)p * n + k], aqk = a[(size_t)q * n + k];
-          a[(size_t)p * n + k] = c * apk - s * aqk;
-          a[(size_t)q * n + k] = s * apk + c * aqk;
-        }
-        for (int k = 0; k < n; ++k) {
-          const double vkp = v[(size_t)k * n + p], vkq = v[(size_t)k * n + q];
-          v[(size_t)k * n + p] = c * vkp - s * vkq;
-          v[(size_t)k * n + q] = s * vkp + c * vkq;
-        }
-      }
+      if (split) continue;
+      w[l] -= shift;
+      e[l] = g;
+      e[m] = 0.0;
+    }
   }
   std::vector<int> ord(n);
   std::iota(ord.begin(), ord.end(), 0);
-  std::stable_sort(ord.begin(), ord.end(),
-                   [&](int x, int y) { return a[(size_t)x * n + x] < a[(size_t)y * n + y]; });
-  std::vector<double> v2((size_t)n * n);
-  w.resize(n);
+  std::stable_sort(ord.begin(), ord.end(), [&](int x1, int y1) { return w[x1] < w[y1]; });
+  std::vector<double> w2(n);
   for (int j = 0; j < n; ++j) {
-    w[j] = a[(size_t)ord[j] * n + ord[j]];
-    for (int i = 0; i < n; ++i) v2[(size_t)i * n + j] = v[(size_t)i * n + ord[j]];
+    w2[j] = w[ord[j]];
+    const double* zr = &z[(size_t)ord[j] * n];
+    for (int i = 0; i < n; ++i) v[(size_t)i * n + j] = zr[i];
   }
-  v.swap(v2);
+  w.swap(w2);
 }
-
 
 namespace {
 
@@ -95,81 +163,76 @@ inline unsigned gsz(int64_t n, int tpb = DBLK) {
   return (unsigned)g;
 }
 
-// G[i][j] = sum_r A_i[r] B_j[r] for the m columns of A (stacked blocks of nsd
-// columns, block stride N*nsd) and the nsd columns of B.  Rows are staged in
-// shared memory; a thread owns CI consecutive columns of A for every j (a
-// CI x nsd register tile: CI + nsd shared reads per CI*nsd FMAs) over the rows
-// of its row group, and the row groups are added in a fixed order.  One
-// partial per CTA.  A non-null `skip` flag that is set makes the kernel write
-// zeros (the conditional second Gram-Schmidt pass).
-constexpr int GTR = 32;
-template <int CI>
-__global__ void __launch_bounds__(DBLK) k_gram(const double* A, int m, const double* B, int nsd, int64_t N,
-                                               int64_t rows_per_cta, double* partial, const int* skip) {
-  extern __shared__ double sm[];
-  double* As = sm;            // [GTR][m]
-  double* Bs = sm + GTR * m;  // [GTR][nsd]
-  const int np = m * nsd;
-  const int ncol = m / CI;                       // column groups
-  const int groups = min(DBLK / ncol, GTR);      // row groups
-  if (skip && *skip) {
-    for (int p = threadIdx.x; p < np; p += DBLK) partial[(int64_t)blockIdx.x * np + p] = 0.0;
-    return;
+// G[i][j] = sum_r A_i[r] B_j[r]: A has m columns (column i is column i % nsd
+// of the block i / nsd; blocks strideA apart, rows of nsd values), B is B0
+// (nsd columns) or [B0 B1] (2 nsd columns), NBC = the number of B columns.
+// GB300 issues two FP64 FMAs per clock per SM, so the kernel only has to keep
+// the FP64 pipe fed: a lane owns one row at a time and CI = 32 / NBC columns
+// of A, so a row costs CI + NBC loads for CI * NBC FMAs and every FMA is
+// useful work (no padded columns).  A warp holds one column group; the eight
+// warps of a CTA cover eight column groups, or split the rows when there are
+// fewer groups, and gridDim.y passes cover the rest of the columns.  Lanes
+// are combined by a reduce-scatter, warps of the same column group through
+// shared memory in a fixed order, and one partial per CTA is written, so the
+// sums are deterministic.  A non-null `skip` flag that is set makes the
+// kernel return at once (the conditional second Gram-Schmidt pass).
+template <int NBC>
+__global__ void __launch_bounds__(DBLK) k_gram(const double* __restrict__ A, int m, int64_t strideA,
+                                               const double* __restrict__ B0, const double* __restrict__ B1, int nsd,
+                                               int64_t N, int64_t rows_per_cta, double* partial, const int* skip) {
+  constexpr int CI = 32 / NBC;
+  if (skip && *skip) return;
+  __shared__ double red[DBLK / 32][32];
+  const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int ncg = (m + CI - 1) / CI;
+  const int cg0 = blockIdx.y * (DBLK / 32);
+  const int ncg_here = min(DBLK / 32, ncg - cg0);
+  const int rg = (DBLK / 32) / ncg_here;  // row groups
+  const int cgl = w % ncg_here, rgi = w / ncg_here;
+  const bool active = rgi < rg;
+  const int cg = cg0 + cgl;
+  const int nq = min(CI, m - cg * CI);  // real columns of this group (warp uniform)
+  const double* ap[CI];
+#pragma unroll
+  for (int q = 0; q < CI; ++q) {
+    const int i = min(cg * CI + q, m - 1);
+    ap[q] = A + (int64_t)(i / nsd) * strideA + (i % nsd);
   }
+  double acc[32];
+#pragma unroll
+  for (int k = 0; k < 32; ++k) acc[k] = 0.0;
   const int64_t r0 = (int64_t)blockIdx.x * rows_per_cta;
   const int64_t r1 = min(r0 + rows_per_cta, N);
-  const int ci = threadIdx.x % ncol, g = threadIdx.x / ncol;
-  const bool active = g < groups;
-  double acc[CI][MAXS];
+  if (active) {
+    for (int64_t r = r0 + (int64_t)rgi * 32 + lane; r < r1; r += (int64_t)rg * 32) {
+      double a[CI], b[NBC];
 #pragma unroll
-  for (int a = 0; a < CI; ++a)
+      for (int q = 0; q < CI; ++q) a[q] = (q < nq) ? ap[q][r * nsd] : 0.0;
 #pragma unroll
-    for (int j = 0; j < MAXS; ++j) acc[a][j] = 0.0;
-  for (int64_t t0 = r0; t0 < r1; t0 += GTR) {
-    const int tr = (int)min((int64_t)GTR, r1 - t0);
-    __syncthreads();
-    const int nb = m / nsd;
-    for (int idx = threadIdx.x; idx < nb * tr * nsd; idx += DBLK) {
-      const int b = idx / (tr * nsd), rem = idx % (tr * nsd), r = rem / nsd, c = rem % nsd;
-      As[r * m + b * nsd + c] = A[(int64_t)b * N * nsd + (t0 + r) * nsd + c];
-    }
-    for (int idx = threadIdx.x; idx < tr * nsd; idx += DBLK) Bs[idx] = B[t0 * nsd + idx];
-    __syncthreads();
-    if (active) {
-      for (int r = g; r < tr; r += groups) {
-        double a[CI];
+      for (int j = 0; j < NBC; ++j) b[j] = (j < nsd) ? B0[r * nsd + j] : B1[r * nsd + j - nsd];
 #pragma unroll
-        for (int q = 0; q < CI; ++q) a[q] = As[r * m + ci * CI + q];
-        const double* brow = &Bs[r * nsd];
+      for (int q = 0; q < CI; ++q)
+        if (q < nq)
 #pragma unroll
-        for (int j = 0; j < MAXS; ++j) {
-          if (j < nsd) {
-            const double bv = brow[j];
-#pragma unroll
-            for (int q = 0; q < CI; ++q) acc[q][j] = fma(a[q], bv, acc[q][j]);
-          }
-        }
-      }
+          for (int j = 0; j < NBC; ++j) acc[q * NBC + j] = fma(a[q], b[j], acc[q * NBC + j]);
     }
   }
+  // lane L ends with entry L = (q, j) = (L / NBC, L % NBC) of the group's tile
+  const double v = qpsig::reduce_scatter64<32>(acc, lane);
+  if (active) red[w][lane] = v;
   __syncthreads();
-  // fixed-order sum over row groups through shared memory (reuses the tiles)
-  double* red = sm;  // [groups][m][nsd]
-  if (active)
-#pragma unroll
-    for (int q = 0; q < CI; ++q)
-      for (int j = 0; j < nsd; ++j) red[((size_t)g * m + ci * CI + q) * nsd + j] = acc[q][j];
-  __syncthreads();
-  for (int p = threadIdx.x; p < np; p += DBLK) {
-    double s = 0.0;
-    for (int q = 0; q < groups; ++q) s += red[(size_t)q * np + p];
-    partial[(int64_t)blockIdx.x * np + p] = s;
+  if (w < ncg_here) {
+    double t = 0.0;
+    for (int g = 0; g < rg; ++g) t += red[g * ncg_here + w][lane];
+    const int q = lane / NBC, j = lane % NBC, i = cg * CI + q;
+    if (q < CI && i < m) partial[(int64_t)blockIdx.x * m * NBC + (int64_t)i * NBC + j] = t;
   }
 }
 
 // out[p] = sum over CTAs of partial[cta][p]: one warp per element, lane l
 // adds CTAs l, l+32, ... and the lanes combine in a fixed butterfly order
-__global__ void k_reduce_partials(const double* partial, int ncta, int np, double* out) {
+__global__ void k_reduce_partials(const double* partial, int ncta, int np, double* out, const int* skip) {
+  if (skip && *skip) return;
   const int lane = threadIdx.x & 31;
   const int wpb = blockDim.x >> 5;
   for (int p = blockIdx.x * wpb + (threadIdx.x >> 5); p < np; p += gridDim.x * wpb) {
@@ -181,63 +244,64 @@ __global__ void k_reduce_partials(const double* partial, int ncta, int np, doubl
   }
 }
 
-// out_k[r][j] (=, -=) sum_i A_k[i-th column][r] C[i][j], for up to 3 (A, out)
-// pairs sharing C (m x nsd, row-major).  Each thread owns LR rows (LR*256
-// apart, so a warp's loads stay contiguous) and keeps LR x nsd accumulators:
-// one shared-memory read of C serves LR FMAs.  out may alias A when m == nsd
-// (a thread reads all its rows before writing them).
-constexpr int LR = 4;
+// out_t[r][0:nsd] = sum_i A_t[column i][r] C[i][0:nsd] for up to 3 (A, out)
+// pairs sharing C (m x nsd, row-major; the m columns are nb consecutive blocks
+// of nsd).  A lane owns one row: per block it loads the row's NSD values
+// (contiguous; 16-byte loads for even NSD, so a warp reads one contiguous
+// span) and does NSD x NSD FMAs against C broadcast from shared memory; the
+// next block's values are loaded before the current ones are used.  The sum
+// runs over (block, column) in order, so results are deterministic.  out may
+// alias a block of A (a lane reads all of its row before writing it).
 struct LinComb {
   const double* A[3];
   double* out[3];
   int n;
 };
-__global__ void __launch_bounds__(DBLK) k_lincomb(LinComb L, int m, int nsd, int64_t N, const double* C, int sub,
-                                                  const int* skip) {
+template <int NSD>
+__device__ __forceinline__ void load_row(const double* __restrict__ p, double (&x)[NSD]) {
+  if constexpr (NSD % 2 == 0) {
+#pragma unroll
+    for (int c = 0; c < NSD / 2; ++c) {
+      const double2 v = reinterpret_cast<const double2*>(p)[c];
+      x[2 * c] = v.x;
+      x[2 * c + 1] = v.y;
+    }
+  } else {
+#pragma unroll
+    for (int c = 0; c < NSD; ++c) x[c] = p[c];
+  }
+}
+template <int NSD>
+__global__ void __launch_bounds__(DBLK) k_lincomb(LinComb L, int nb, int64_t N, const double* C, const int* skip) {
   if (skip && *skip) return;
   __shared__ __align__(16) double Cs[MAXM * MAXS];
-  for (int i = threadIdx.x; i < m * nsd; i += DBLK) Cs[i] = C[i];
+  for (int i = threadIdx.x; i < nb * NSD * NSD; i += DBLK) Cs[i] = C[i];
   __syncthreads();
-  const int nb = m / nsd;
-  const int64_t span = (int64_t)DBLK * LR;
-  for (int64_t base = (int64_t)blockIdx.x * span; base < N; base += (int64_t)gridDim.x * span) {
-    int64_t rr[LR];
-    bool ok[LR];
-#pragma unroll
-    for (int q = 0; q < LR; ++q) {
-      rr[q] = base + threadIdx.x + (int64_t)q * DBLK;
-      ok[q] = rr[q] < N;
-    }
+  const int64_t sA = N * NSD;
+  for (int64_t r = blockIdx.x * (int64_t)DBLK + threadIdx.x; r < N; r += (int64_t)gridDim.x * DBLK) {
     for (int t = 0; t < L.n; ++t) {
-      double acc[LR][MAXS];
+      const double* a = L.A[t] + r * NSD;
+      double acc[NSD], x[NSD], xn[NSD];
 #pragma unroll
-      for (int q = 0; q < LR; ++q)
-#pragma unroll
-        for (int j = 0; j < MAXS; ++j) acc[q][j] = 0.0;
+      for (int j = 0; j < NSD; ++j) acc[j] = 0.0;
+      load_row<NSD>(a, x);
       for (int b = 0; b < nb; ++b) {
-        const double* ab = L.A[t] + (int64_t)b * N * nsd;
-        for (int c = 0; c < nsd; ++c) {
-          double x[LR];
+        if (b + 1 < nb) load_row<NSD>(a + (int64_t)(b + 1) * sA, xn);
+        const double* cb = Cs + b * NSD * NSD;
 #pragma unroll
-          for (int q = 0; q < LR; ++q) x[q] = ok[q] ? ab[rr[q] * nsd + c] : 0.0;
-          const double* crow = &Cs[(b * nsd + c) * nsd];
+        for (int c = 0; c < NSD; ++c)
 #pragma unroll
-          for (int j = 0; j < MAXS; ++j) {
-            if (j < nsd) {
-              const double cv = crow[j];
+          for (int j = 0; j < NSD; ++j) acc[j] = fma(x[c], cb[c * NSD + j], acc[j]);
 #pragma unroll
-              for (int q = 0; q < LR; ++q) acc[q][j] = fma(x[q], cv, acc[q][j]);
-            }
-          }
-        }
+        for (int c = 0; c < NSD; ++c) x[c] = xn[c];
       }
+      double* o = L.out[t] + r * NSD;
+      if constexpr (NSD % 2 == 0) {
 #pragma unroll
-      for (int q = 0; q < LR; ++q) {
-        if (!ok[q]) continue;
-        double* o = L.out[t] + rr[q] * nsd;
+        for (int c = 0; c < NSD / 2; ++c) reinterpret_cast<double2*>(o)[c] = make_double2(acc[2 * c], acc[2 * c + 1]);
+      } else {
 #pragma unroll
-        for (int j = 0; j < MAXS; ++j)
-          if (j < nsd) o[j] = sub ? o[j] - acc[q][j] : acc[q][j];
+        for (int j = 0; j < NSD; ++j) o[j] = acc[j];
       }
     }
   }
@@ -281,16 +345,79 @@ __global__ void k_chol_inv(const double* G, int nsd, double* Rinv) {
     for (int j = 0; j < nsd; ++j) Rinv[i * nsd + j] = Ri[i][j];
 }
 
-// second Gram-Schmidt pass needed?  Yes when a column lost more than half of
-// its norm in the first pass (G0 before, G1 after; diagonals).
-__global__ void k_need_second_pass(const double* G0, const double* G1, int nsd, int* skip) {
-  if (threadIdx.x || blockIdx.x) return;
-  int need = 0;
-  for (int j = 0; j < nsd; ++j) {
-    const double a = G0[j * nsd + j], b = G1[j * nsd + j];
-    if (!(b > 0.25 * a)) need = 1;
+// Coefficients of the fused classical Gram-Schmidt + Cholesky-QR update of a
+// new block U_b (nsd columns) against the m orthonormal columns before it.
+// X = [U_0 .. U_b]^T U_b ((m + nsd) x nsd): C = X[0:m], G0 = X[m:m+nsd].
+// G1 = G0 - C^T C is the Gram matrix of U_b - U C.  When every column kept
+// more than half of its norm (G1_jj > G0_jj / 4, so G1 carries no
+// cancellation) the update is fused with the Cholesky factor G1 = R^T R:
+// K = [-C R^-1; R^-1], and U_b <- [U_0 .. U_b] K orthogonalises and
+// normalises in one pass.  Otherwise K = [-C; I] (plain Gram-Schmidt) and
+// *skip2 = 0 asks for a second pass (mode 1), which always fuses.  Mode 1
+// returns at once when *skip2 is set.  A vanishing Cholesky pivot (a
+// dependent column) gives a zero column, as in k_chol_inv.
+__global__ void k_cgs_coef(const double* X, int m, int nsd, double* K, int* skip2, int mode) {
+  if (mode == 1 && *skip2) return;
+  __shared__ double G[MAXS][MAXS], Ri[MAXS][MAXS];
+  __shared__ int need;
+  for (int idx = threadIdx.x; idx < nsd * nsd; idx += blockDim.x) {
+    const int i = idx / nsd, j = idx % nsd;
+    double g = X[(m + i) * nsd + j];
+    for (int k = 0; k < m; ++k) g -= X[k * nsd + i] * X[k * nsd + j];
+    G[i][j] = g;
   }
-  *skip = need ? 0 : 1;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    int nd = 0;
+    if (mode == 0)
+      for (int j = 0; j < nsd; ++j)
+        if (!(G[j][j] > 0.25 * X[(m + j) * nsd + j])) nd = 1;
+    need = nd;
+    if (mode == 0) *skip2 = nd ? 0 : 1;
+    if (!nd) {
+      double R[MAXS][MAXS];
+      for (int i = 0; i < nsd; ++i)
+        for (int j = 0; j < nsd; ++j) R[i][j] = Ri[i][j] = 0.0;
+      for (int j = 0; j < nsd; ++j) {
+        double dj = G[j][j];
+        for (int k = 0; k < j; ++k) dj -= R[k][j] * R[k][j];
+        if (!(dj > 1e-28 * fabs(G[j][j])) || !(dj > 1e-300)) continue;  // zero row of R
+        R[j][j] = sqrt(dj);
+        for (int i = j + 1; i < nsd; ++i) {
+          double t = G[j][i];
+          for (int k = 0; k < j; ++k) t -= R[k][j] * R[k][i];
+          R[j][i] = t / R[j][j];
+        }
+      }
+      for (int j = nsd - 1; j >= 0; --j) {
+        if (R[j][j] == 0.0) continue;
+        Ri[j][j] = 1.0 / R[j][j];
+        for (int i = j - 1; i >= 0; --i) {
+          if (R[i][i] == 0.0) continue;
+          double t = 0.0;
+          for (int k = i + 1; k <= j; ++k) t += R[i][k] * Ri[k][j];
+          Ri[i][j] = -t / R[i][i];
+        }
+      }
+    }
+  }
+  __syncthreads();
+  const bool fuse = !need;
+  for (int idx = threadIdx.x; idx < (m + nsd) * nsd; idx += blockDim.x) {
+    const int i = idx / nsd, j = idx % nsd;
+    double v;
+    if (i < m) {
+      if (fuse) {
+        v = 0.0;
+        for (int k = 0; k <= j; ++k) v -= X[i * nsd + k] * Ri[k][j];
+      } else {
+        v = -X[i * nsd + j];
+      }
+    } else {
+      v = fuse ? Ri[i - m][j] : (i - m == j ? 1.0 : 0.0);
+    }
+    K[idx] = v;
+  }
 }
 
 struct StepParams {
@@ -504,28 +631,48 @@ struct Dav {
   double* blk(double* X, int b) const { return X + (int64_t)b * N * nsd; }
 };
 
-int gram(Dav& d, const double* A, int m, const double* B, double* out_dev, const int* skip = nullptr) {
-  const int ci = (m % 4 == 0) ? 4 : (m % 2 == 0) ? 2 : 1;
-  const int groups = std::min(DBLK / (m / ci), GTR);
-  const size_t shm = std::max((size_t)GTR * (m + d.nsd), (size_t)groups * m * d.nsd) * sizeof(double);
-  static bool attr_set = false;  // shared memory above 48 KB needs an opt-in (at most 64 KB here)
-  if (!attr_set) {
-    cudaFuncSetAttribute(k_gram<4>, cudaFuncAttributeMaxDynamicSharedMemorySize, 96 * 1024);
-    cudaFuncSetAttribute(k_gram<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, 96 * 1024);
-    cudaFuncSetAttribute(k_gram<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, 96 * 1024);
-    attr_set = true;
+// device small-matrix area (doubles)
+constexpr int OFF_X = 0;                     // Gram outputs, up to MAXM x 2 MAXS
+constexpr int OFF_K = 2 * MAXM * MAXS;       // update coefficients, MAXM x MAXS
+constexpr int OFF_Y = 3 * MAXM * MAXS;       // Ritz coefficients y, MAXM x MAXS
+constexpr int OFF_G = 4 * MAXM * MAXS;       // nsd x nsd Gram block
+constexpr int OFF_RINV = OFF_G + MAXS * MAXS;
+constexpr int OFF_FLAG = OFF_RINV + MAXS * MAXS;
+constexpr int SMALL_DOUBLES = OFF_FLAG + 8;
+
+// out (m x nbc) = A^T [B0 (B1)] with A = m columns of consecutive blocks
+int gram(Dav& d, const double* A, int m, const double* B0, const double* B1, double* out, const int* skip = nullptr) {
+  const int nbc = d.nsd * (B1 ? 2 : 1);
+  const int ci = 32 / nbc;
+  const int ncg = (m + ci - 1) / ci;
+  const dim3 grid(d.ncta, (ncg + DBLK / 32 - 1) / (DBLK / 32));
+  const int64_t sA = d.N * d.nsd;
+#define QP_GRAM_CASE(NB)                                                                                      \
+  case NB:                                                                                                    \
+    k_gram<NB><<<grid, DBLK, 0, d.st>>>(A, m, sA, B0, B1, d.nsd, d.N, d.rows_per_cta, d.part, skip); \
+    break;
+  switch (nbc) {
+    QP_GRAM_CASE(1)
+    QP_GRAM_CASE(2)
+    QP_GRAM_CASE(3)
+    QP_GRAM_CASE(4)
+    QP_GRAM_CASE(5)
+    QP_GRAM_CASE(6)
+    QP_GRAM_CASE(7)
+    QP_GRAM_CASE(8)
+    QP_GRAM_CASE(10)
+    QP_GRAM_CASE(12)
+    QP_GRAM_CASE(14)
+    QP_GRAM_CASE(16)
+    default:
+      return -1;
   }
-  if (ci == 4)
-    k_gram<4><<<d.ncta, DBLK, shm, d.st>>>(A, m, B, d.nsd, d.N, d.rows_per_cta, d.part, skip);
-  else if (ci == 2)
-    k_gram<2><<<d.ncta, DBLK, shm, d.st>>>(A, m, B, d.nsd, d.N, d.rows_per_cta, d.part, skip);
-  else
-    k_gram<1><<<d.ncta, DBLK, shm, d.st>>>(A, m, B, d.nsd, d.N, d.rows_per_cta, d.part, skip);
-  k_reduce_partials<<<gsz((int64_t)m * d.nsd * 32), DBLK, 0, d.st>>>(d.part, d.ncta, m * d.nsd, out_dev);
+#undef QP_GRAM_CASE
+  k_reduce_partials<<<gsz((int64_t)m * nbc * 32), DBLK, 0, d.st>>>(d.part, d.ncta, m * nbc, out, skip);
   return 0;
 }
 
-void lincomb(Dav& d, int m, const double* C, int sub, const double* A0, double* O0, const double* A1 = nullptr,
+void lincomb(Dav& d, int m, const double* C, const double* A0, double* O0, const double* A1 = nullptr,
              double* O1 = nullptr, const double* A2 = nullptr, double* O2 = nullptr, const int* skip = nullptr) {
   LinComb L{};
   L.A[0] = A0;
@@ -541,32 +688,49 @@ void lincomb(Dav& d, int m, const double* C, int sub, const double* A0, double* 
     L.out[2] = O2;
     L.n = 3;
   }
-  k_lincomb<<<gsz((d.N + LR - 1) / LR), DBLK, 0, d.st>>>(L, m, d.nsd, d.N, C, sub, skip);
+  const int nb = m / d.nsd;
+  const unsigned grid = std::min<unsigned>(gsz(d.N), 152 * 8);
+  switch (d.nsd) {
+#define QP_LC_CASE(NS) \
+  case NS:             \
+    k_lincomb<NS><<<grid, DBLK, 0, d.st>>>(L, nb, d.N, C, skip); \
+    break;
+    QP_LC_CASE(1)
+    QP_LC_CASE(2)
+    QP_LC_CASE(3)
+    QP_LC_CASE(4)
+    QP_LC_CASE(5)
+    QP_LC_CASE(6)
+    QP_LC_CASE(7)
+    QP_LC_CASE(8)
+#undef QP_LC_CASE
+  }
 }
 
-// orthonormalise block b against blocks 0..b-1 (classical Gram-Schmidt, a
-// second pass when the first lost more than half of a column's norm) and
-// within itself (CholQR2)
+// orthonormalise block b against blocks 0..b-1 and within itself: one fused
+// Gram-Schmidt + Cholesky-QR pass (k_cgs_coef), a second one when the first
+// lost more than half of a column's norm, then a Cholesky-QR pass on the
+// block alone (CholQR2)
 void orthonormalise(Dav& d, int b) {
   double* Ub = d.blk(d.U, b);
-  double* cbuf = d.small;  // m x nsd
-  double* G = d.small + MAXM * MAXS;
-  double* Rinv = d.small + 2 * MAXM * MAXS;
-  double* G0 = d.small + 4 * MAXM * MAXS;
-  int* skip = (int*)(d.small + 5 * MAXM * MAXS);
+  double* X = d.small + OFF_X;
+  double* K = d.small + OFF_K;
+  double* G = d.small + OFF_G;
+  double* Rinv = d.small + OFF_RINV;
+  int* skip2 = (int*)(d.small + OFF_FLAG);
+  const int m = b * d.nsd, m1 = m + d.nsd;
   if (b > 0) {
-    gram(d, Ub, d.nsd, Ub, G0);
-    gram(d, d.U, b * d.nsd, Ub, cbuf);
-    lincomb(d, b * d.nsd, cbuf, 1, d.U, Ub);
-    gram(d, Ub, d.nsd, Ub, G);
-    k_need_second_pass<<<1, 1, 0, d.st>>>(G0, G, d.nsd, skip);
-    gram(d, d.U, b * d.nsd, Ub, cbuf, skip);
-    lincomb(d, b * d.nsd, cbuf, 1, d.U, Ub, nullptr, nullptr, nullptr, nullptr, skip);
+    gram(d, d.U, m1, Ub, nullptr, X);
+    k_cgs_coef<<<1, 128, 0, d.st>>>(X, m, d.nsd, K, skip2, 0);
+    lincomb(d, m1, K, d.U, Ub);
+    gram(d, d.U, m1, Ub, nullptr, X, skip2);
+    k_cgs_coef<<<1, 128, 0, d.st>>>(X, m, d.nsd, K, skip2, 1);
+    lincomb(d, m1, K, d.U, Ub, nullptr, nullptr, nullptr, nullptr, skip2);
   }
-  for (int pass = 0; pass < 2; ++pass) {
-    gram(d, Ub, d.nsd, Ub, G);
+  for (int pass = (b > 0) ? 1 : 0; pass < 2; ++pass) {
+    gram(d, Ub, d.nsd, Ub, nullptr, G);
     k_chol_inv<<<1, 1, 0, d.st>>>(G, d.nsd, Rinv);
-    lincomb(d, d.nsd, Rinv, 0, Ub, Ub);
+    lincomb(d, d.nsd, Rinv, Ub, Ub);
   }
 }
 
@@ -638,8 +802,8 @@ extern "C" int qpgpu_davidson_hs2(qpgpu_ctx* c, double* u_in, int64_t dim_in, do
   const size_t blkn = (size_t)N * nsd;
   if (dev_alloc(&d.U, blkn * itermax) != cudaSuccess || dev_alloc(&d.W, blkn * itermax) != cudaSuccess ||
       dev_alloc(&d.S, blkn * itermax) != cudaSuccess || dev_alloc(&d.R, blkn) != cudaSuccess ||
-      dev_alloc(&d.u32, blkn) != cudaSuccess || dev_alloc(&d.part, (size_t)d.ncta * MAXM * MAXS) != cudaSuccess ||
-      dev_alloc(&d.small, (size_t)6 * MAXM * MAXS) != cudaSuccess) {
+      dev_alloc(&d.u32, blkn) != cudaSuccess || dev_alloc(&d.part, (size_t)d.ncta * MAXM * 2 * MAXS) != cudaSuccess ||
+      dev_alloc(&d.small, (size_t)SMALL_DOUBLES) != cudaSuccess) {
     cudaGetLastError();
     return qpgpu_fail(c, QPGPU_ERR_NOMEM, "Davidson work arrays do not fit on the device");
   }
@@ -686,7 +850,7 @@ extern "C" int qpgpu_davidson_hs2(qpgpu_ctx* c, double* u_in, int64_t dim_in, do
   const double sz2sz = Sz * (Sz - 1.0), expected_s2 = Sz * (Sz + 1.0);
   const int mmax = itermax * nsd;
   std::vector<double> h((size_t)mmax * mmax, 0.0), s_((size_t)mmax * mmax, 0.0);
-  std::vector<double> hcol((size_t)mmax * nsd), scol((size_t)mmax * nsd);
+  std::vector<double> hcol((size_t)mmax * nsd), scol((size_t)mmax * nsd), hscol((size_t)mmax * 2 * nsd);
   std::vector<double> lambda(mmax), s2(mmax), y, wv, res(MAXS, 0.0), partial((size_t)d.ncta * MAXS);
   int n_sigma = 0, shift2 = 0, trace_n = 0;
   bool converged = false, failed = false;
@@ -723,12 +887,16 @@ extern "C" int qpgpu_davidson_hs2(qpgpu_ctx* c, double* u_in, int64_t dim_in, do
       ++n_sigma;
       prof.mark(DavProf::SIGMA);
       // new Gram columns
-      gram(d, d.U, shift2, d.blk(d.W, b), d.small);
-      gram(d, d.U, shift2, d.blk(d.S, b), d.small + MAXM * MAXS);
-      QP_CUDA(c, cudaMemcpyAsync(hcol.data(), d.small, (size_t)shift2 * nsd * sizeof(double), cudaMemcpyDeviceToHost, st));
-      QP_CUDA(c, cudaMemcpyAsync(scol.data(), d.small + MAXM * MAXS, (size_t)shift2 * nsd * sizeof(double),
+      // h(:, new) and s(:, new) in one pass over U: X = U^T [W_b S_b]
+      gram(d, d.U, shift2, d.blk(d.W, b), d.blk(d.S, b), d.small + OFF_X);
+      QP_CUDA(c, cudaMemcpyAsync(hscol.data(), d.small + OFF_X, (size_t)shift2 * 2 * nsd * sizeof(double),
                                  cudaMemcpyDeviceToHost, st));
       QP_CUDA(c, cudaStreamSynchronize(st));
+      for (int i = 0; i < shift2; ++i)
+        for (int j = 0; j < nsd; ++j) {
+          hcol[(size_t)i * nsd + j] = hscol[(size_t)i * 2 * nsd + j];
+          scol[(size_t)i * nsd + j] = hscol[(size_t)i * 2 * nsd + nsd + j];
+        }
       prof.mark(DavProf::GRAM);
       for (int i = 0; i < shift2; ++i)
         for (int j = 0; j < nsd; ++j) {
@@ -744,7 +912,7 @@ extern "C" int qpgpu_davidson_hs2(qpgpu_ctx* c, double* u_in, int64_t dim_in, do
           hs[(size_t)i * shift2 + j] = h[(size_t)i * mmax + j];
           ss[(size_t)i * shift2 + j] = s_[(size_t)i * mmax + j];
         }
-      qp_jacobi(hs, shift2, wv, y);
+      qp_eigh(hs, shift2, wv, y);
       for (int k = 0; k < shift2; ++k) lambda[k] = wv[k];
       // S^2 of the Ritz vectors (:289-301): s2_k = y_k^T s y_k + S_z(S_z-1)
       for (int k = 0; k < shift2; ++k) {
@@ -776,10 +944,10 @@ extern "C" int qpgpu_davidson_hs2(qpgpu_ctx* c, double* u_in, int64_t dim_in, do
       std::vector<double> ycoef((size_t)shift2 * nsd);
       for (int i = 0; i < shift2; ++i)
         for (int j = 0; j < nsd; ++j) ycoef[(size_t)i * nsd + j] = y[(size_t)i * shift2 + j];
-      double* ydev = d.small + 3 * MAXM * MAXS;
+      double* ydev = d.small + OFF_Y;
       prof.mark(DavProf::HOST);
       QP_CUDA(c, cudaMemcpyAsync(ydev, ycoef.data(), ycoef.size() * sizeof(double), cudaMemcpyHostToDevice, st));
-      lincomb(d, shift2, ydev, 0, d.U, d.blk(d.U, iter), d.W, d.blk(d.W, iter), d.S, d.blk(d.S, iter));
+      lincomb(d, shift2, ydev, d.U, d.blk(d.U, iter), d.W, d.blk(d.W, iter), d.S, d.blk(d.S, iter));
       prof.mark(DavProf::RITZ);
       // Davidson step and residual norms (:386-395)
       StepParams sp{};
@@ -846,9 +1014,9 @@ extern "C" int qpgpu_davidson_hs2(qpgpu_ctx* c, double* u_in, int64_t dim_in, do
     std::vector<double> ycoef((size_t)shift2 * nsd);
     for (int i = 0; i < shift2; ++i)
       for (int j = 0; j < nsd; ++j) ycoef[(size_t)i * nsd + j] = y[(size_t)i * shift2 + j];
-    double* ydev = d.small + 3 * MAXM * MAXS;
+    double* ydev = d.small + OFF_Y;
     QP_CUDA(c, cudaMemcpyAsync(ydev, ycoef.data(), ycoef.size() * sizeof(double), cudaMemcpyHostToDevice, st));
-    lincomb(d, shift2, ydev, 0, d.U, d.R);
+    lincomb(d, shift2, ydev, d.U, d.R);
     k_copy<<<gsz((int64_t)blkn), DBLK, 0, st>>>(d.R, d.U, (int64_t)blkn);
     prof.mark(DavProf::RESTART);
     for (int i = 0; i < mmax; ++i)

@@ -499,4 +499,4 @@ __device__ __forceinline__ float qp_mlp_forward(const float* P, const float* f) 
 
 // small symmetric eigenproblem on the host (davidson.cu): ascending
 // eigenvalues, eigenvectors in the columns of v (row-major n x n)
-void qp_jacobi(std::vector<double> a, int n, std::vector<double>& w, std::vector<double>& v);
+void qp_eigh(std::vector<double> a, int n, std::vector<double>& w, std::vector<double>& v);
