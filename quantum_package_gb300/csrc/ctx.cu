@@ -193,6 +193,10 @@ int qpgpu_create(int n_mo, int n_alpha, int n_beta, int n_int, qpgpu_ctx** out) 
     delete c;
     return QPGPU_ERR_CUDA;
   }
+  if (cudaDeviceGetAttribute(&c->n_sm, cudaDevAttrMultiProcessorCount, c->device) != cudaSuccess || c->n_sm < 1) {
+    cudaGetLastError();
+    c->n_sm = 152;
+  }
   *out = c;
   return QPGPU_OK;
 }

@@ -802,7 +802,7 @@ extern "C" int qpgpu_davidson_hs2(qpgpu_ctx* c, double* u_in, int64_t dim_in, do
   const size_t blkn = (size_t)N * nsd;
   if (dev_alloc(&d.U, blkn * itermax) != cudaSuccess || dev_alloc(&d.W, blkn * itermax) != cudaSuccess ||
       dev_alloc(&d.S, blkn * itermax) != cudaSuccess || dev_alloc(&d.R, blkn) != cudaSuccess ||
-      dev_alloc(&d.u32, blkn) != cudaSuccess || dev_alloc(&d.part, (size_t)d.ncta * MAXM * 2 * MAXS) != cudaSuccess ||
+      dev_alloc(&d.u32, (size_t)N * qp_pad_states(nsd)) != cudaSuccess || dev_alloc(&d.part, (size_t)d.ncta * MAXM * 2 * MAXS) != cudaSuccess ||
       dev_alloc(&d.small, (size_t)SMALL_DOUBLES) != cudaSuccess) {
     cudaGetLastError();
     return qpgpu_fail(c, QPGPU_ERR_NOMEM, "Davidson work arrays do not fit on the device");
@@ -880,9 +880,9 @@ extern "C" int qpgpu_davidson_hs2(qpgpu_ctx* c, double* u_in, int64_t dim_in, do
       prof.mark(DavProf::ORTHO);
       // sigma on block b
       const int prec = (mixed && iter > 1) ? QPGPU_FP32 : QPGPU_FP64;
-      if (prec == QPGPU_FP32) qp_to_float(d.blk(d.U, b), d.u32, (int64_t)blkn, st);
+      if (prec == QPGPU_FP32) qp_to_float(d.blk(d.U, b), d.u32, N, nsd, qp_pad_states(nsd), st);
       int rc = qp_sigma_launch(c, &c->items, d.blk(d.W, b), d.blk(d.S, b), d.blk(d.U, b), d.u32, nsd, prec, st, 0,
-                               (int)N, 0, 1);
+                               (int)N, 0, 1, qp_pad_states(nsd));
       if (rc) return rc;
       ++n_sigma;
       prof.mark(DavProf::SIGMA);

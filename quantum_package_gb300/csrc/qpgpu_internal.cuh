@@ -305,6 +305,8 @@ struct SigmaItems {
   double* pv = nullptr;       // partial sums (n_items, n_st)
   double* ps = nullptr;
   size_t partial_cap = 0;
+  int sig32_variant[18] = {-1, -1, -1, -1, -1, -1, -1, -1, -1,
+                           -1, -1, -1, -1, -1, -1, -1, -1, -1};  // tuned FP32 shape per n_st (+9: padded rows)
   void free_all() {
     void* ps_[] = {row_nitems, row_item0, item_row, item_sub, multi_rows, pv, ps};
     for (void* p : ps_)
@@ -314,6 +316,7 @@ struct SigmaItems {
     partial_cap = 0;
     n_items = 0;
     n_multi = 0;
+    for (int& v : sig32_variant) v = -1;
   }
 };
 
@@ -354,6 +357,7 @@ struct MlpState {
 struct qpgpu_ctx {
   std::mutex mu;
   int device = 0;
+  int n_sm = 152;  // streaming multiprocessors of the device
   cudaStream_t stream = nullptr;
   std::string last_error;
 
@@ -439,13 +443,17 @@ int qp_build_pairs(qpgpu_ctx* c);      // pairs.cu
 void qp_free_dets(qpgpu_ctx* c);       // index.cu
 void qp_free_pairs(qpgpu_ctx* c);      // pairs.cu
 int qp_build_sigma_items(qpgpu_ctx* c, SigmaItems* it);  // sigma.cu
+// u32_ld: floats between FP32 rows (0: n_st; or n_st padded by qp_pad_states)
 int qp_sigma_launch(qpgpu_ctx* c, SigmaItems* it, double* v, double* s, const double* u, const float* u32, int nst,
-                    int precision, cudaStream_t st, int row_lo, int row_hi, int row_first, int row_step);
+                    int precision, cudaStream_t st, int row_lo, int row_hi, int row_first, int row_step,
+                    int u32_ld = 0);
+// FP32 row length that keeps a row of n_st coefficients in one 32-byte sector
+inline int qp_pad_states(int nst) { return nst <= 1 ? 1 : nst <= 2 ? 2 : nst <= 4 ? 4 : 8; }
 void qp_to_bilinear(const double* u0, int64_t ld, const int* order, double* ut, float* ut32, int nst, int64_t N,
                     cudaStream_t st);
 void qp_from_bilinear(const double* vt, int64_t ld, const int* order, double* v0, int nst, int64_t N,
                       cudaStream_t st);
-void qp_to_float(const double* x, float* y, int64_t n, cudaStream_t st);
+void qp_to_float(const double* x, float* y, int64_t N, int nst, int ld, cudaStream_t st);
 
 // records a named event on the context stream when profiling is on
 inline void qp_mark(qpgpu_ctx* c, const char* name) {

@@ -8,6 +8,9 @@
 // result is deterministic.  u is laid out (N_det, N_st) with states fastest,
 // as u_t(N_st, N_det) in the reference (:27-41), so the N_st coefficients of a
 // connected determinant J are one contiguous load.
+#include <algorithm>
+#include <cstdio>
+
 #include "qpgpu_internal.cuh"
 #include "sigma_device.cuh"
 
@@ -31,7 +34,8 @@ struct SigArgs {
   const int* row_nitems;
   int64_t n_items;
   const double* u;   // (N, NST) FP64
-  const float* u32;  // (N, NST) FP32 (precision FP32)
+  const float* u32;  // (N, u32_ld) FP32 (precision FP32): rows u32_ld floats apart
+  int u32_ld;
   double* v;
   double* s;
   double* pv;  // partial sums (n_items, NST)
@@ -124,15 +128,52 @@ __global__ void __launch_bounds__(SBLK) k_sigma64(SigArgs a) {
   }
 }
 
+// (column, value) pairs of one trip: lane's pairs e0, e0+32, ...; past the
+// end of the chunk the row's own column with value 0 (a harmless gather)
+__device__ __forceinline__ void load_trip32(const SigArgs& a, int64_t e0, int64_t end, int k, int (&col)[UNR32],
+                                            float (&hv)[UNR32]) {
+#pragma unroll
+  for (int q = 0; q < UNR32; ++q) {
+    const int64_t e = e0 + 32 * q;
+    col[q] = e < end ? __ldg(&a.colidx[e]) : k;
+    hv[q] = e < end ? __ldg(&a.val32[e]) : 0.f;
+  }
+}
+
+// Kahan-compensated sum += hv * u32[col] for the trip's pairs
+template <int NST, int NP, int LD, bool V8>
+__device__ __forceinline__ void accumulate32(const SigArgs& a, const int (&col)[UNR32], const float (&hv)[UNR32],
+                                             float (&sum)[NP], float (&cmp)[NP]) {
+#pragma unroll
+  for (int q = 0; q < UNR32; ++q) {
+    float x[NST];
+    load_row_ld<NST, LD, V8>(a.u32, col[q], x);
+#pragma unroll
+    for (int st = 0; st < NST; ++st) {
+      const float y = __fmaf_rn(hv[q], x[st], -cmp[st]);
+      const float t = __fadd_rn(sum[st], y);
+      cmp[st] = __fsub_rn(__fsub_rn(t, sum[st]), y);
+      sum[st] = t;
+    }
+  }
+}
+
 // FP32 matrix elements x FP32 coefficients with Kahan-compensated lane sums;
 // lanes are combined as float-float pairs, and only the owner lane of each
 // state converts to FP64 and adds the FP64 diagonal term.
-template <int NST>
-__global__ void __launch_bounds__(SBLK) k_sigma32(SigArgs a) {
+//
+// The kernel is bound by load latency (each coefficient gather waits on its
+// column index).  With PIPE the next trip's (column, value) pairs are loaded
+// one trip ahead of the current trip's gathers, at the price of registers,
+// hence occupancy; which launch shape hides the latency best depends on the
+// row lengths, so it is chosen by timing (tune_sigma32).  Every shape gives
+// bit-identical sums: each lane sees the same pairs in the same order.
+template <int NST, bool PIPE, int BS, int LD, bool V8>
+__global__ void __launch_bounds__(BS) k_sigma32(SigArgs a) {
   constexpr int NP = Pow2<NST>::v;
   const int lane = threadIdx.x & 31;
-  const int64_t warp = ((int64_t)blockIdx.x * SBLK + threadIdx.x) >> 5;
-  const int64_t nwarp = ((int64_t)gridDim.x * SBLK) >> 5;
+  const int64_t warp = ((int64_t)blockIdx.x * BS + threadIdx.x) >> 5;
+  const int64_t nwarp = ((int64_t)gridDim.x * BS) >> 5;
   for (int64_t it = warp; it < a.n_items; it += nwarp) {
     const int k = a.item_row[it];
     if (!row_selected(a, k)) continue;
@@ -143,19 +184,27 @@ __global__ void __launch_bounds__(SBLK) k_sigma32(SigArgs a) {
     float sum[NP], cmp[NP];
 #pragma unroll
     for (int st = 0; st < NP; ++st) sum[st] = cmp[st] = 0.f;
+    int col[UNR32];
+    float hv[UNR32];
+    if (PIPE) load_trip32(a, beg + lane, end, k, col, hv);
     for (int64_t e0 = beg + lane; e0 < end; e0 += 32 * UNR32) {
-      int col[UNR32];
-      float hv[UNR32];
+      if (PIPE) {
+        int ncol[UNR32];
+        float nhv[UNR32];
+        load_trip32(a, e0 + 32 * UNR32, end, k, ncol, nhv);
+        accumulate32<NST, NP, LD, V8>(a, col, hv, sum, cmp);
 #pragma unroll
-      for (int q = 0; q < UNR32; ++q) {
-        const int64_t e = e0 + 32 * q;
-        col[q] = e < end ? __ldg(&a.colidx[e]) : k;
-        hv[q] = e < end ? __ldg(&a.val32[e]) : 0.f;
+        for (int q = 0; q < UNR32; ++q) {
+          col[q] = ncol[q];
+          hv[q] = nhv[q];
+        }
+        continue;
       }
+      load_trip32(a, e0, end, k, col, hv);
 #pragma unroll
       for (int q = 0; q < UNR32; ++q) {
         float x[NST];
-        load_row<NST>(a.u32, col[q], x);
+        load_row_ld<NST, LD, V8>(a.u32, col[q], x);
 #pragma unroll
         for (int st = 0; st < NST; ++st) {
           const float y = __fmaf_rn(hv[q], x[st], -cmp[st]);
@@ -181,7 +230,7 @@ __global__ void __launch_bounds__(SBLK) k_sigma32(SigArgs a) {
       for (int64_t e = sb + lane; e < se; e += 32) {
         const float sv = __ldg(&a.s2val[e]);  // +-1: products are exact
         float x[NST];
-        load_row<NST>(a.u32, __ldg(&a.s2col[e]), x);
+        load_row_ld<NST, LD, V8>(a.u32, __ldg(&a.s2col[e]), x);
 #pragma unroll
         for (int st = 0; st < NST; ++st) {
           float s, err;
@@ -253,9 +302,10 @@ __global__ void k_from_bilinear(const double* vt, int64_t ld, const int* order, 
   }
 }
 
-__global__ void k_to_float(const double* x, float* y, int64_t n) {
-  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
-    y[i] = (float)x[i];
+// y (N rows of ld floats) <- x (N rows of nst doubles)
+__global__ void k_to_float(const double* x, float* y, int64_t N, int nst, int ld) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < N * nst; i += (int64_t)gridDim.x * blockDim.x)
+    y[(i / nst) * ld + i % nst] = (float)x[i];
 }
 
 inline unsigned gsz(int64_t n, int tpb) {
@@ -265,12 +315,109 @@ inline unsigned gsz(int64_t n, int tpb) {
   return (unsigned)g;
 }
 
+// FP32 launch shapes tried by the tuner: kernel variant, CTA size and grid
+// policy (0: one warp per work item; n: a persistent grid of n CTAs per SM)
+struct Sig32Shape {
+  bool pipe;
+  int bs, ctas_per_sm;
+};
+constexpr Sig32Shape kSig32Shapes[] = {{false, 256, 0}, {false, 128, 0}, {false, 64, 0}, {true, 256, 0}};
+constexpr int kNSig32Shapes = sizeof(kSig32Shapes) / sizeof(kSig32Shapes[0]);
+
+template <int NST, int LD, bool V8>
+void launch_sigma32_ld(const SigArgs& a, int variant, cudaStream_t st, int n_sm) {
+  const Sig32Shape sh = kSig32Shapes[variant];
+  int64_t g = (a.n_items * 32 + sh.bs - 1) / sh.bs;
+  if (sh.ctas_per_sm) g = std::min<int64_t>(g, (int64_t)sh.ctas_per_sm * n_sm);
+  g = std::max<int64_t>(1, std::min<int64_t>(g, 65535LL * 32));
+  const unsigned grid = (unsigned)g;
+  switch (variant) {
+    case 1: k_sigma32<NST, false, 128, LD, V8><<<grid, 128, 0, st>>>(a); break;
+    case 2: k_sigma32<NST, false, 64, LD, V8><<<grid, 64, 0, st>>>(a); break;
+    case 3: k_sigma32<NST, true, 256, LD, V8><<<grid, 256, 0, st>>>(a); break;
+    default: k_sigma32<NST, false, 256, LD, V8><<<grid, 256, 0, st>>>(a); break;
+  }
+}
+
+// dense rows (u32_ld == NST) or rows padded to 4 / 8 floats; rows of 8 floats
+// on a 32-byte aligned array are read with one 256-bit load each
 template <int NST>
-void launch_sigma(const SigArgs& a, int precision, unsigned grid, cudaStream_t st) {
+void launch_sigma32(const SigArgs& a, int variant, cudaStream_t st, int n_sm) {
+  constexpr int P = Pow2<NST>::v;
+  const bool a32 = ((uintptr_t)a.u32 & 31) == 0;
+  if constexpr (P == 8) {
+    if (a.u32_ld == 8 && a32) {
+      launch_sigma32_ld<NST, 8, true>(a, variant, st, n_sm);
+      return;
+    }
+    if constexpr (NST == 8) {
+      k_sigma32<8, false, 256, 8, false><<<(unsigned)std::max<int64_t>(1, std::min<int64_t>(
+                                               (a.n_items * 32 + 255) / 256, 65535LL * 32)),
+                                           256, 0, st>>>(a);
+      return;
+    }
+  }
+  if constexpr (P != NST && P == 4) {
+    if (a.u32_ld == 4) {
+      launch_sigma32_ld<NST, 4, false>(a, variant, st, n_sm);
+      return;
+    }
+  }
+  if constexpr (NST != 8) launch_sigma32_ld<NST, NST, false>(a, variant, st, n_sm);
+}
+
+template <int NST>
+void launch_sigma(const SigArgs& a, int precision, unsigned grid, cudaStream_t st, int n_sm, int variant) {
   if (precision == QPGPU_FP32)
-    k_sigma32<NST><<<grid, SBLK, 0, st>>>(a);
+    launch_sigma32<NST>(a, variant < 0 ? 0 : variant, st, n_sm);
   else
     k_sigma64<NST><<<grid, SBLK, 0, st>>>(a);
+}
+
+void launch_any(const SigArgs& a, int nst, int precision, unsigned grid, cudaStream_t st, int n_sm, int variant) {
+  switch (nst) {
+    case 1: launch_sigma<1>(a, precision, grid, st, n_sm, variant); break;
+    case 2: launch_sigma<2>(a, precision, grid, st, n_sm, variant); break;
+    case 3: launch_sigma<3>(a, precision, grid, st, n_sm, variant); break;
+    case 4: launch_sigma<4>(a, precision, grid, st, n_sm, variant); break;
+    case 5: launch_sigma<5>(a, precision, grid, st, n_sm, variant); break;
+    case 6: launch_sigma<6>(a, precision, grid, st, n_sm, variant); break;
+    case 7: launch_sigma<7>(a, precision, grid, st, n_sm, variant); break;
+    default: launch_sigma<8>(a, precision, grid, st, n_sm, variant); break;
+  }
+}
+
+// Times every FP32 launch shape on this determinant set (two launches each,
+// the second timed with events on the caller's stream) and keeps the fastest
+// for n_st.  Runs once per determinant set and n_st, on the first FP32 call;
+// the outputs it writes are those of the call itself.
+int tune_sigma32(qpgpu_ctx* c, SigmaItems* it, const SigArgs& a, int nst, cudaStream_t st, int slot) {
+  cudaEvent_t e0, e1;
+  if (cudaEventCreate(&e0) != cudaSuccess || cudaEventCreate(&e1) != cudaSuccess) {
+    cudaGetLastError();
+    return qpgpu_fail(c, QPGPU_ERR_CUDA, "cudaEventCreate failed while tuning the FP32 sigma");
+  }
+  int best = 0;
+  float best_ms = 1e30f;
+  for (int v = 0; v < kNSig32Shapes; ++v) {
+    launch_any(a, nst, QPGPU_FP32, 1, st, c->n_sm, v);
+    cudaEventRecord(e0, st);
+    launch_any(a, nst, QPGPU_FP32, 1, st, c->n_sm, v);
+    cudaEventRecord(e1, st);
+    if (cudaEventSynchronize(e1) != cudaSuccess) break;
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, e0, e1);
+    if (c->profile) fprintf(stderr, "[qpgpu] sigma32 n_st=%d row=%d floats shape %d: %.3f ms\n", nst, a.u32_ld, v, ms);
+    if (ms < best_ms) {
+      best_ms = ms;
+      best = v;
+    }
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  QP_CUDA(c, cudaGetLastError());
+  it->sig32_variant[slot] = best;
+  return 0;
 }
 
 }  // namespace
@@ -325,8 +472,12 @@ static int ensure_partials(qpgpu_ctx* c, SigmaItems* it, int nst) {
 }
 
 int qp_sigma_launch(qpgpu_ctx* c, SigmaItems* it, double* v, double* s, const double* u, const float* u32, int nst,
-                    int precision, cudaStream_t st, int row_lo, int row_hi, int row_first, int row_step) {
+                    int precision, cudaStream_t st, int row_lo, int row_hi, int row_first, int row_step,
+                    int u32_ld) {
   if (nst < 1 || nst > 8) return qpgpu_fail(c, QPGPU_ERR_ARG, "n_st must be in 1..8 per sigma block");
+  if (u32_ld <= 0) u32_ld = nst;
+  if (u32_ld != nst && !(u32_ld == qp_pad_states(nst) && (((uintptr_t)u32) & 31) == 0))
+    return qpgpu_fail(c, QPGPU_ERR_ARG, "FP32 rows must be n_st floats apart, or padded to 4/8 and 32-byte aligned");
   if (precision == QPGPU_FP32 && !u32) return qpgpu_fail(c, QPGPU_ERR_ARG, "FP32 sigma needs u_t32");
   int rc = ensure_partials(c, it, nst);
   if (rc) return rc;
@@ -347,6 +498,7 @@ int qp_sigma_launch(qpgpu_ctx* c, SigmaItems* it, double* v, double* s, const do
   a.n_items = it->n_items;
   a.u = u;
   a.u32 = u32;
+  a.u32_ld = u32_ld;
   a.v = v;
   a.s = s;
   a.pv = it->pv;
@@ -356,16 +508,12 @@ int qp_sigma_launch(qpgpu_ctx* c, SigmaItems* it, double* v, double* s, const do
   a.row_first = row_first;
   a.row_step = row_step;
   const unsigned grid = gsz(it->n_items * 32, SBLK);
-  switch (nst) {
-    case 1: launch_sigma<1>(a, precision, grid, st); break;
-    case 2: launch_sigma<2>(a, precision, grid, st); break;
-    case 3: launch_sigma<3>(a, precision, grid, st); break;
-    case 4: launch_sigma<4>(a, precision, grid, st); break;
-    case 5: launch_sigma<5>(a, precision, grid, st); break;
-    case 6: launch_sigma<6>(a, precision, grid, st); break;
-    case 7: launch_sigma<7>(a, precision, grid, st); break;
-    default: launch_sigma<8>(a, precision, grid, st); break;
+  const int slot = nst + (u32_ld != nst ? 9 : 0);
+  if (precision == QPGPU_FP32 && it->sig32_variant[slot] < 0) {
+    rc = tune_sigma32(c, it, a, nst, st, slot);
+    if (rc) return rc;
   }
+  launch_any(a, nst, precision, grid, st, c->n_sm, it->sig32_variant[slot]);
   if (it->n_multi > 0)
     k_sigma_combine<<<gsz((int64_t)it->n_multi * nst, 256), 256, 0, st>>>(a, it->multi_rows, it->row_item0,
                                                                          it->n_multi, nst);
@@ -383,8 +531,8 @@ void qp_from_bilinear(const double* vt, int64_t ld, const int* order, double* v0
   k_from_bilinear<<<gsz(N * nst, 256), 256, 0, st>>>(vt, ld, order, v0, nst, N);
 }
 
-void qp_to_float(const double* x, float* y, int64_t n, cudaStream_t st) {
-  k_to_float<<<gsz(n, 256), 256, 0, st>>>(x, y, n);
+void qp_to_float(const double* x, float* y, int64_t N, int nst, int ld, cudaStream_t st) {
+  k_to_float<<<gsz(N * nst, 256), 256, 0, st>>>(x, y, N, nst, ld);
 }
 
 // ---------------------------------------------------------------------------
@@ -459,6 +607,7 @@ extern "C" int qpgpu_sigma_bilinear_noalloc(qpgpu_ctx* c, double* v_t, double* s
   a.n_items = it->n_items;
   a.u = u_t;
   a.u32 = u_t32;
+  a.u32_ld = n_st;
   a.v = v_t;
   a.s = s_t;
   a.pv = scratch;  // every slot read by k_sigma_combine is written earlier in the same call
@@ -469,16 +618,7 @@ extern "C" int qpgpu_sigma_bilinear_noalloc(qpgpu_ctx* c, double* v_t, double* s
   a.row_step = 1;
   cudaStream_t st = stream ? (cudaStream_t)stream : c->stream;
   const unsigned grid = gsz(it->n_items * 32, SBLK);
-  switch (n_st) {
-    case 1: launch_sigma<1>(a, precision, grid, st); break;
-    case 2: launch_sigma<2>(a, precision, grid, st); break;
-    case 3: launch_sigma<3>(a, precision, grid, st); break;
-    case 4: launch_sigma<4>(a, precision, grid, st); break;
-    case 5: launch_sigma<5>(a, precision, grid, st); break;
-    case 6: launch_sigma<6>(a, precision, grid, st); break;
-    case 7: launch_sigma<7>(a, precision, grid, st); break;
-    default: launch_sigma<8>(a, precision, grid, st); break;
-  }
+  launch_any(a, n_st, precision, grid, st, c->n_sm, it->sig32_variant[n_st]);
   if (it->n_multi > 0)
     k_sigma_combine<<<gsz((int64_t)it->n_multi * n_st, 256), 256, 0, st>>>(a, it->multi_rows, it->row_item0,
                                                                           it->n_multi, n_st);

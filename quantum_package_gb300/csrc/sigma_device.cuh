@@ -121,4 +121,41 @@ __device__ __forceinline__ void load_row(const float* u, int64_t col, float (&x)
   }
 }
 
+// FP32 coefficients of row col from a layout whose rows are LD floats apart
+// (LD = NST, or NST padded to 4 or 8 so that a row sits in one 32-byte
+// sector: 16-byte loads, then an 8-byte and a 4-byte load for the rest)
+template <int NST, int LD, bool V8 = false>
+__device__ __forceinline__ void load_row_ld(const float* u, int64_t col, float (&x)[NST]) {
+  const float* p = u + col * LD;
+  if constexpr (LD == 8 && V8) {
+    // one 32-byte load (sm_100+ 256-bit vector load; p is 32-byte aligned):
+    // a single L2 request per row instead of two
+    float t[8];
+    asm("ld.global.nc.v8.f32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
+        : "=f"(t[0]), "=f"(t[1]), "=f"(t[2]), "=f"(t[3]), "=f"(t[4]), "=f"(t[5]), "=f"(t[6]), "=f"(t[7])
+        : "l"(p));
+#pragma unroll
+    for (int i = 0; i < NST; ++i) x[i] = t[i];
+  } else if constexpr (LD % 4 == 0) {
+    constexpr int N4 = NST / 4, R = NST % 4;
+#pragma unroll
+    for (int i = 0; i < N4; ++i) {
+      const float4 t = __ldg(reinterpret_cast<const float4*>(p) + i);
+      x[4 * i] = t.x;
+      x[4 * i + 1] = t.y;
+      x[4 * i + 2] = t.z;
+      x[4 * i + 3] = t.w;
+    }
+    if constexpr (R >= 2) {
+      const float2 t = __ldg(reinterpret_cast<const float2*>(p + 4 * N4));
+      x[4 * N4] = t.x;
+      x[4 * N4 + 1] = t.y;
+    }
+    if constexpr (R % 2 == 1) x[NST - 1] = __ldg(p + NST - 1);
+  } else {
+    load_row<NST>(u, col, x);
+  }
+}
+
+
 }  // namespace qpsig
