@@ -307,6 +307,92 @@ __global__ void __launch_bounds__(DBLK) k_lincomb(LinComb L, int nb, int64_t N, 
   }
 }
 
+// Float-float (hi + lo) form of a double, built with integer and FP32
+// instructions only: hi keeps the top 24 bits of the significand
+// (truncated), lo the next 23 (the last 6 bits, below 2^-46 |x|, are
+// dropped), so hi + lo carries about 47 significant bits.  |x| below 2^-126
+// gives (0, 0) and below 2^-80 lo = 0, absolute errors far below anything a
+// Davidson vector resolves.  Finite |x| < 2^127 is assumed (normalised CI
+// vectors and their sigma).
+__device__ __forceinline__ void split_ff(double x, float& hi, float& lo) {
+  const unsigned long long b = (unsigned long long)__double_as_longlong(x);
+  const unsigned h32 = (unsigned)(b >> 32), l32 = (unsigned)b;
+  const unsigned sign = h32 & 0x80000000u;
+  const int e = (int)((h32 >> 20) & 0x7ffu);
+  const int fe = e - 896;  // float biased exponent of hi (e - 1023 + 127)
+  if (fe <= 0) {
+    hi = 0.f;
+    lo = 0.f;
+    return;
+  }
+  hi = __uint_as_float(sign | ((unsigned)fe << 23) | ((h32 & 0xfffffu) << 3) | (l32 >> 29));
+  const int se = e - 942;  // biased exponent of 2^(e - 1069)
+  if (se <= 0) {
+    lo = 0.f;
+    return;
+  }
+  const float r = __fsub_rn(__uint_as_float(0x4B000000u | ((l32 & 0x1fffffffu) >> 6)), 8388608.0f);
+  lo = __fmul_rn(r, __uint_as_float((unsigned)se << 23));
+  if (sign) lo = -lo;
+}
+
+// k_lincomb in float-float arithmetic on the FP32 pipes (GB300 issues 64
+// FP32 FMAs for each FP64 FMA): each product of split operands is formed
+// exactly for hi*hi (an FMA gives its rounding error) plus the hi*lo cross
+// terms, and the running sum is kept as an unevaluated pair with Knuth's
+// TwoSum on the high part.  About 47-bit accuracy; used for the Ritz vectors
+// U y, W y, S y of the mixed-precision Davidson, whose W and S come from the
+// FP32 sigma on most iterations.  Same row ownership, loads and summation
+// order as k_lincomb.
+template <int NSD>
+__global__ void __launch_bounds__(DBLK) k_lincomb_ff(LinComb L, int nb, int64_t N, const double* C) {
+  __shared__ float2 Cs[MAXM * MAXS];
+  for (int i = threadIdx.x; i < nb * NSD * NSD; i += DBLK) {
+    float h, l;
+    split_ff(C[i], h, l);
+    Cs[i] = make_float2(h, l);
+  }
+  __syncthreads();
+  const int64_t sA = N * NSD;
+  for (int64_t r = blockIdx.x * (int64_t)DBLK + threadIdx.x; r < N; r += (int64_t)gridDim.x * DBLK) {
+    for (int t = 0; t < L.n; ++t) {
+      const double* a = L.A[t] + r * NSD;
+      float ah[NSD], al[NSD];
+      double x[NSD], xn[NSD];
+#pragma unroll
+      for (int j = 0; j < NSD; ++j) ah[j] = al[j] = 0.f;
+      load_row<NSD>(a, x);
+      for (int b = 0; b < nb; ++b) {
+        if (b + 1 < nb) load_row<NSD>(a + (int64_t)(b + 1) * sA, xn);
+        const float2* cb = Cs + b * NSD * NSD;
+#pragma unroll
+        for (int c = 0; c < NSD; ++c) {
+          float xh, xl;
+          split_ff(x[c], xh, xl);
+#pragma unroll
+          for (int j = 0; j < NSD; ++j) {
+            const float2 cv = cb[c * NSD + j];
+            const float p = __fmul_rn(xh, cv.x);
+            float pe = __fmaf_rn(xh, cv.x, -p);
+            pe = __fmaf_rn(xh, cv.y, pe);
+            pe = __fmaf_rn(xl, cv.x, pe);
+            const float s = __fadd_rn(ah[j], p);
+            const float bb = __fsub_rn(s, ah[j]);
+            const float err = __fadd_rn(__fsub_rn(ah[j], __fsub_rn(s, bb)), __fsub_rn(p, bb));
+            ah[j] = s;
+            al[j] = __fadd_rn(al[j], __fadd_rn(err, pe));
+          }
+        }
+#pragma unroll
+        for (int c = 0; c < NSD; ++c) x[c] = xn[c];
+      }
+      double* o = L.out[t] + r * NSD;
+#pragma unroll
+      for (int j = 0; j < NSD; ++j) o[j] = (double)ah[j] + (double)al[j];
+    }
+  }
+}
+
 // Cholesky G = R^T R (nsd x nsd) and Rinv = R^-1 (row-major, upper), one
 // thread.  A vanishing pivot (dependent column) gives a zero column.
 __global__ void k_chol_inv(const double* G, int nsd, double* Rinv) {
@@ -707,6 +793,37 @@ void lincomb(Dav& d, int m, const double* C, const double* A0, double* O0, const
   }
 }
 
+// the same linear combination of three (A, out) pairs in float-float
+// arithmetic (mixed-precision Ritz vectors)
+void lincomb_ff(Dav& d, int m, const double* C, const double* A0, double* O0, const double* A1, double* O1,
+                const double* A2, double* O2) {
+  LinComb L{};
+  L.A[0] = A0;
+  L.out[0] = O0;
+  L.A[1] = A1;
+  L.out[1] = O1;
+  L.A[2] = A2;
+  L.out[2] = O2;
+  L.n = 3;
+  const int nb = m / d.nsd;
+  const unsigned grid = std::min<unsigned>(gsz(d.N), 152 * 8);
+  switch (d.nsd) {
+#define QP_LCF_CASE(NS) \
+  case NS:              \
+    k_lincomb_ff<NS><<<grid, DBLK, 0, d.st>>>(L, nb, d.N, C); \
+    break;
+    QP_LCF_CASE(1)
+    QP_LCF_CASE(2)
+    QP_LCF_CASE(3)
+    QP_LCF_CASE(4)
+    QP_LCF_CASE(5)
+    QP_LCF_CASE(6)
+    QP_LCF_CASE(7)
+    QP_LCF_CASE(8)
+#undef QP_LCF_CASE
+  }
+}
+
 // orthonormalise block b against blocks 0..b-1 and within itself: one fused
 // Gram-Schmidt + Cholesky-QR pass (k_cgs_coef), a second one when the first
 // lost more than half of a column's norm, then a Cholesky-QR pass on the
@@ -947,7 +1064,10 @@ extern "C" int qpgpu_davidson_hs2(qpgpu_ctx* c, double* u_in, int64_t dim_in, do
       double* ydev = d.small + OFF_Y;
       prof.mark(DavProf::HOST);
       QP_CUDA(c, cudaMemcpyAsync(ydev, ycoef.data(), ycoef.size() * sizeof(double), cudaMemcpyHostToDevice, st));
-      lincomb(d, shift2, ydev, d.U, d.blk(d.U, iter), d.W, d.blk(d.W, iter), d.S, d.blk(d.S, iter));
+      if (mixed)  // Ritz vectors in float-float (the FP64 list is projection, eigensolve, GS, norms)
+        lincomb_ff(d, shift2, ydev, d.U, d.blk(d.U, iter), d.W, d.blk(d.W, iter), d.S, d.blk(d.S, iter));
+      else
+        lincomb(d, shift2, ydev, d.U, d.blk(d.U, iter), d.W, d.blk(d.W, iter), d.S, d.blk(d.S, iter));
       prof.mark(DavProf::RITZ);
       // Davidson step and residual norms (:386-395)
       StepParams sp{};
@@ -985,10 +1105,13 @@ extern "C" int qpgpu_davidson_hs2(qpgpu_ctx* c, double* u_in, int64_t dim_in, do
         if (r > 1e8 || !std::isfinite(r)) failed = true;  // 'Davidson failed' (:404-409)
       }
       // fallback: a state whose residual (the reference's measure, from the
-      // diagonal correction) fell by less than 5% in two consecutive learned
-      // steps goes back to the diagonal step for the rest of the run
+      // diagonal correction) failed to fall by at least 5% in two consecutive
+      // learned steps goes back to the diagonal step for the rest of the run.
+      // The first iteration of a restart cycle is not judged: its residual
+      // comes from the re-contracted basis (and, in mixed precision, from the
+      // cycle's first FP64 sigma), not from the preceding step.
       for (int k = 0; k < nst; ++k) {
-        if (mlp_on[k]) {
+        if (mlp_on[k] && iter > 1) {
           strikes[k] = (res[k] > 0.95 * prev_res[k]) ? strikes[k] + 1 : 0;
           if (strikes[k] >= 2) {
             mlp_on[k] = false;
