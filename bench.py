@@ -55,7 +55,8 @@ def parse():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-davidson", action="store_true", help="skip the Davidson time-to-E block")
     ap.add_argument("--davidson-only", action="store_true", help="only the Davidson block (profiling)")
-    ap.add_argument("--n-states-diag", type=int, default=6, help="N_st_diag of the Davidson runs")
+    ap.add_argument("--n-states-diag", type=int, default=8, help="N_st_diag of the Davidson runs")
+    ap.add_argument("--davidson-sze-max", type=int, default=10, help="davidson_sze_max of the Davidson runs")
     return ap.parse_args()
 
 
@@ -205,6 +206,7 @@ def workload_config(prob):
 
 
 N_STATES_DIAG = 8
+SZE_MAX = 8
 E_TOL = 1e-6
 
 
@@ -232,10 +234,11 @@ def davidson_block(prob, wf):
     from quantum_package_gb300 import FP32, FP64
     N = prob.n_det
     u = _guess(N, prob.seed)
-    kw = dict(n_states=N_STATES, s2_eig=False, max_iter=400)
+    kw = dict(n_states=N_STATES, s2_eig=False, max_iter=400, davidson_sze_max=SZE_MAX)
     tight = wf.davidson_diag_hs2(u, threshold=1e-12, **kw)
     e_ref = tight["energies"][:N_STATES]
-    out = {"n_states": N_STATES, "n_states_diag": N_STATES_DIAG, "threshold": 1e-10, "e_tol_ha": E_TOL,
+    out = {"n_states": N_STATES, "n_states_diag": N_STATES_DIAG, "davidson_sze_max": SZE_MAX,
+           "threshold": 1e-10, "e_tol_ha": E_TOL,
            "fp64_reference_energies": e_ref.tolist(),
            "note": "s2_eig off: the seeded space is not spin complete; energies are electronic (Ha)"}
 
@@ -266,16 +269,22 @@ def davidson_block(prob, wf):
     wf.set_dets(prob.dets)
     out["training"] = {"stages": train, "wall_s": time.perf_counter() - t0,
                        "note": "training on earlier determinant sets; not part of time-to-E"}
+    # learned step in place of the diagonal step (preconditioner=1), and as an
+    # extra direction in the slots of the non-target Ritz vectors (=2)
     run("plain_fp64_learned", preconditioner=1)
     run("mixed_learned", precision=FP32, preconditioner=1)
+    run("mixed_learned_extra", precision=FP32, preconditioner=2)
+    a, b = out["plain_fp64"]["time_to_E_s"], out["mixed"]["time_to_E_s"]
+    out["speedup_mixed_vs_plain"] = (a / b) if (a and b) else None
     a, b = out["plain_fp64"]["time_to_E_s"], out["mixed_learned"]["time_to_E_s"]
     out["speedup_mixed_learned_vs_plain"] = (a / b) if (a and b) else None
     return out
 
 
 def run_ours(args):
-    global N_STATES_DIAG
+    global N_STATES_DIAG, SZE_MAX
     N_STATES_DIAG = args.n_states_diag
+    SZE_MAX = args.davidson_sze_max
     import torch
     rank, world, local = dist_env()
     torch.cuda.set_device(local)

@@ -134,7 +134,9 @@ typedef struct qpgpu_davidson_params {
   double threshold;         /* threshold_davidson on the squared step norm (1e-12) */
   int32_t precision;        /* QPGPU_FP64, or QPGPU_FP32: FP32 sigma with an FP64 sigma at each restart */
   int32_t defect_every;     /* FP32 mode: restart (FP64 sigma) at least every k iterations (0: sze_max) */
-  int32_t preconditioner;   /* 0: the reference's diagonal step; 1: learned (MLP) step with fallback */
+  int32_t preconditioner;   /* 0: the reference's diagonal step; 1: learned (MLP) step in place of the
+                               diagonal one, with fallback; 2: learned step as an extra direction in the
+                               slot of Ritz vector n_states + k (states k < n_states_diag - n_states) */
   int32_t max_iter;         /* cap on sigma applications (0: 1000) */
   int32_t collect_every;    /* > 0: capture training pairs every k iterations (from the 2nd) */
   int32_t collect_max;      /* captures kept (default 8) */

@@ -548,13 +548,19 @@ __global__ void __launch_bounds__(DBLK) k_step(double* Un, const double* Wn, con
   }
 }
 
-// Davidson step with the learned preconditioner: the reference's diagonal
-// correction d (whose squared norm stays the convergence measure) is scaled
-// per determinant by the MLP's multiplier g for the states flagged in
-// p.mlp_mask; other states take d unchanged.
+// Davidson step with the learned preconditioner.  d_k is the reference's
+// diagonal correction of Ritz vector k (its squared norm stays the
+// convergence measure); g_k the MLP's per-determinant multiplier.
+//   replace (extra == 0): state k flagged in mlp_mask takes g_k d_k instead
+//     of d_k;
+//   extra (extra == 1): the correction slot of the non-target Ritz vector
+//     nst + k takes g_k d_k, so the subspace receives both d_k and g_k d_k
+//     for a flagged target state k and the Rayleigh-Ritz step weighs them: a
+//     poor network costs a little of the block's extra directions instead of
+//     the target's own step.
 __global__ void __launch_bounds__(DBLK) k_step_mlp(double* Un, const double* Wn, const double* Sn, const double* hjj,
                                                    const float4* feat, const float* P, int64_t N, StepParams p,
-                                                   unsigned mlp_mask, double* partial) {
+                                                   unsigned mlp_mask, int extra, double* partial) {
   __shared__ float Ps[QP_MLP_NPARAM];
   __shared__ double red[MAXS][DBLK / 32];
   for (int i = threadIdx.x; i < QP_MLP_NPARAM; i += DBLK) Ps[i] = P[i];
@@ -565,16 +571,29 @@ __global__ void __launch_bounds__(DBLK) k_step_mlp(double* Un, const double* Wn,
   for (int64_t r = blockIdx.x * (int64_t)DBLK + threadIdx.x; r < N; r += (int64_t)gridDim.x * DBLK) {
     const double h = hjj[r];
     const float4 st = feat[r];
-    for (int k = 0; k < p.nsd; ++k) {
+    double learned[MAXS];  // g_k d_k of the flagged target states (extra mode)
+#pragma unroll
+    for (int k = 0; k < MAXS; ++k) {
+      learned[k] = 0.0;
+      if (k >= p.nsd) continue;
       const int64_t x = r * p.nsd + k;
       const double u = Un[x];
       const double res = p.lambda[k] * u - Wn[x];
       const double d = res * (1.0 + p.s2[k] * u - Sn[x] - p.sz2sz) / fmax(h - p.lambda[k], 1e-2);
       double v = d;
-      if ((mlp_mask >> k) & 1u) {
+      if (k < p.nst && ((mlp_mask >> k) & 1u)) {
         float f[QP_MLP_IN];
         qp_features(st, h - p.lambda[k], u, res, d, f);
-        v = d * (double)qp_mlp_forward(Ps, f);
+        const double gd = d * (double)qp_mlp_forward(Ps, f);
+        if (extra)
+          learned[k] = gd;
+        else
+          v = gd;
+      }
+      if (extra && k >= p.nst && ((mlp_mask >> (k - p.nst)) & 1u)) {
+#pragma unroll
+        for (int q = 0; q < MAXS; ++q)
+          if (q == k - p.nst) v = learned[q];
       }
       Un[x] = v;
       if (k < p.nst) acc[k] = fma(d, d, acc[k]);
@@ -899,6 +918,8 @@ extern "C" int qpgpu_davidson_hs2(qpgpu_ctx* c, double* u_in, int64_t dim_in, do
   if (nst < 1 || nsd < nst || nsd > MAXS || dim_in < N || prm->davidson_sze_max < 1 ||
       (prm->precision != QPGPU_FP64 && prm->precision != QPGPU_FP32))
     return qpgpu_fail(c, QPGPU_ERR_ARG, "bad Davidson parameters (1 <= n_states <= n_states_diag <= 8)");
+  if (prm->preconditioner < 0 || prm->preconditioner > 2)
+    return qpgpu_fail(c, QPGPU_ERR_ARG, "preconditioner must be 0 (diagonal), 1 (learned) or 2 (learned, extra direction)");
   if ((int64_t)nsd * 3 > N) return qpgpu_fail(c, QPGPU_ERR_ARG, "N_st_diag*3 > sze (diagonalization_hs2.irp.f:110)");
   int itermax = std::max(3, (int)std::min<int64_t>(prm->davidson_sze_max, N / nsd));
   while (itermax * nsd > MAXM) --itermax;
@@ -926,14 +947,16 @@ extern "C" int qpgpu_davidson_hs2(qpgpu_ctx* c, double* u_in, int64_t dim_in, do
   }
   cudaStream_t st = d.st;
   // learned preconditioner and training capture
-  const bool use_mlp = prm->preconditioner == 1;
+  const bool use_mlp = prm->preconditioner == 1 || prm->preconditioner == 2;
   if (use_mlp && (!c->mlp.ready || !c->d_detfeat))
     return qpgpu_fail(c, QPGPU_ERR_STATE, "learned preconditioner requested but the MLP is not initialised");
   bool mlp_on[MAXS] = {false};
   int strikes[MAXS] = {0};
   double prev_res[MAXS];
   for (int k = 0; k < MAXS; ++k) prev_res[k] = INFINITY;
-  for (int k = 0; k < nst; ++k) mlp_on[k] = use_mlp;
+  // extra mode: state k's learned correction uses the slot of Ritz vector nst + k
+  const int mlp_extra = prm->preconditioner == 2;
+  for (int k = 0; k < nst; ++k) mlp_on[k] = use_mlp && (!mlp_extra || nst + k < nsd);
   int n_fallback = 0;
   const int collect_every = prm->collect_every > 0 ? prm->collect_every : 0;
   const int collect_max = collect_every ? std::max(1, std::min(prm->collect_max > 0 ? prm->collect_max : 8, 64 / nst)) : 0;
@@ -1089,7 +1112,7 @@ extern "C" int qpgpu_davidson_hs2(qpgpu_ctx* c, double* u_in, int64_t dim_in, do
         if (mlp_on[k]) mask |= 1u << k;
       if (mask)
         k_step_mlp<<<d.ncta, DBLK, 0, st>>>(d.blk(d.U, iter), d.blk(d.W, iter), d.blk(d.S, iter), c->d_hdiag,
-                                            (const float4*)c->d_detfeat, c->mlp.params, N, sp, mask, d.part);
+                                            (const float4*)c->d_detfeat, c->mlp.params, N, sp, mask, mlp_extra, d.part);
       else
         k_step<<<d.ncta, DBLK, 0, st>>>(d.blk(d.U, iter), d.blk(d.W, iter), d.blk(d.S, iter), c->d_hdiag, N, sp, d.part);
       QP_CUDA(c, cudaGetLastError());

@@ -158,7 +158,9 @@ class Wavefunction:
         """davidson_diag_hs2 (diagonalization_hs2.irp.f:1-49) on this determinant set.
 
         u_in: (N_st_diag, N) guess vectors (all of them, seeded by the caller).
-        preconditioner=1 uses the learned step (see mlp_*); collect_every > 0
+        preconditioner=1 uses the learned step (see mlp_*) in place of the
+        diagonal one; preconditioner=2 adds it as an extra direction (in the
+        correction slot of Ritz vector n_states + k); collect_every > 0
         captures training pairs for it.  Returns dict(energies, s2, vectors,
         n_sigma, converged, n_fallback, n_samples, trace) with electronic energies.
         """

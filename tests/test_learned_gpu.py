@@ -47,13 +47,17 @@ def test_learned_preconditioner_gain_and_same_energies(staged, capsys):
     kw = dict(n_states=NST, threshold=1e-12, s2_eig=False, max_iter=500)
     diag = wf.davidson_diag_hs2(u, **kw)
     learned = wf.davidson_diag_hs2(u, preconditioner=1, **kw)
-    assert diag["converged"] and learned["converged"]
+    extra = wf.davidson_diag_hs2(u, preconditioner=2, **kw)
+    assert diag["converged"] and learned["converged"] and extra["converged"]
     np.testing.assert_allclose(learned["energies"][:NST], diag["energies"][:NST], rtol=0, atol=1e-9)
+    np.testing.assert_allclose(extra["energies"][:NST], diag["energies"][:NST], rtol=0, atol=1e-9)
     with capsys.disabled():
         print(f"\n[learned preconditioner] sigma applications: diagonal {diag['n_sigma']}, "
-              f"learned {learned['n_sigma']} (fallbacks {learned['n_fallback']})")
+              f"learned in place {learned['n_sigma']} (fallbacks {learned['n_fallback']}), "
+              f"learned as extra direction {extra['n_sigma']}")
     # no more than a modest regression allowed, whatever the draw
     assert learned["n_sigma"] <= 1.25 * diag["n_sigma"]
+    assert extra["n_sigma"] <= 1.15 * diag["n_sigma"]
 
 
 def test_bad_network_falls_back(staged):
