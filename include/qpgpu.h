@@ -55,6 +55,8 @@ typedef struct qpgpu_info {
   double ref_energy;      /* ref_bitmask_energy */
   int64_t device_bytes;   /* device memory held by the context */
   int64_t n_split_rows;   /* rows whose pairs span several sigma work chunks */
+  int32_t direct_sigma;   /* 1: pairs not stored, sigma enumerates them at each call */
+  int32_t reserved;
 } qpgpu_info;
 
 /* Context for one orbital space; replaces the IRPF90 providers N_int,
@@ -65,6 +67,22 @@ int qpgpu_create(int n_mo, int n_alpha, int n_beta, int n_int, qpgpu_ctx** out);
 int qpgpu_destroy(qpgpu_ctx* ctx);
 const char* qpgpu_last_error(qpgpu_ctx* ctx);
 int qpgpu_get_info(qpgpu_ctx* ctx, qpgpu_info* info);
+
+/* How sigma reaches the connected pairs (no counterpart in the reference,
+ * which recomputes every matrix element at each call, u0Hu0.irp.f:177-444).
+ * QPGPU_SIGMA_STORED: qpgpu_set_dets stores the pairs and their FP64 / FP32
+ * elements once, and sigma streams them (the fast path).  QPGPU_SIGMA_DIRECT:
+ * nothing is stored; every sigma enumerates the pairs again from the
+ * bilinear index and evaluates the Slater rules in FP64, as the reference
+ * does, for determinant sets whose pairs do not fit in device memory (FP32
+ * requests run in FP64; qpgpu_connected_pairs, the no-alloc sigma and
+ * batches need stored pairs).  QPGPU_SIGMA_AUTO (default): stored unless the
+ * pairs would leave less than 1/16 of the device memory free.  Takes effect at
+ * the next qpgpu_set_dets. */
+#define QPGPU_SIGMA_AUTO 0
+#define QPGPU_SIGMA_STORED 1
+#define QPGPU_SIGMA_DIRECT 2
+int qpgpu_set_sigma_mode(qpgpu_ctx* ctx, int mode);
 
 /* Integrals (host).  h_pq: n_mo x n_mo column-major, symmetric
  * (mo_mono_elec_integral, src/Integrals_Monoelec/mo_mono_ints.irp.f:1-26).

@@ -643,7 +643,8 @@ int qpgpu_batch_create(qpgpu_ctx* const* ctxs, int n, qpgpu_batch** out) {
   if (!ctxs || !out || n < 1 || n > 256) return QPGPU_ERR_ARG;
   *out = nullptr;
   for (int i = 0; i < n; ++i)
-    if (!ctxs[i] || !ctxs[i]->have_pairs || ctxs[i]->device != ctxs[0]->device) return QPGPU_ERR_STATE;
+    if (!ctxs[i] || !ctxs[i]->have_pairs || ctxs[i]->direct || ctxs[i]->device != ctxs[0]->device)
+      return QPGPU_ERR_STATE;
   qpgpu_batch* B = new qpgpu_batch();
   B->ctx.assign(ctxs, ctxs + n);
   B->np = n;

@@ -235,10 +235,22 @@ int qpgpu_get_info(qpgpu_ctx* c, qpgpu_info* info) {
   int64_t b = 0;
   if (c->have_ints) b += 8 * (n * (n + 1) / 2) * (n * (n + 1) / 2 + 1) / 2 + 8 * (6 * n * n + 2 * n * n * n);
   if (c->have_dets) b += N * (16 * c->nint + 4 * 8) + 8 * (int64_t)(c->Ua + c->Ub) * c->nint;
-  if (c->have_pairs) b += P * 16 + c->P_s2 * 8 + N * 28;
+  if (c->have_pairs && !c->direct) b += P * 16 + c->P_s2 * 8 + N * 28;
+  if (c->have_pairs && c->direct) b += N * 24;
   b += (int64_t)c->work_bytes;
   info->device_bytes = b;
   info->n_split_rows = c->items.n_multi;
+  info->direct_sigma = c->direct ? 1 : 0;
+  info->reserved = 0;
+  return QPGPU_OK;
+}
+
+int qpgpu_set_sigma_mode(qpgpu_ctx* c, int mode) {
+  if (!c) return QPGPU_ERR_ARG;
+  if (mode != QPGPU_SIGMA_AUTO && mode != QPGPU_SIGMA_STORED && mode != QPGPU_SIGMA_DIRECT)
+    return qpgpu_fail(c, QPGPU_ERR_ARG, "sigma mode must be QPGPU_SIGMA_AUTO, _STORED or _DIRECT");
+  Lock l(c->mu);
+  c->sigma_mode = mode;
   return QPGPU_OK;
 }
 
@@ -338,7 +350,7 @@ int qpgpu_set_dets(qpgpu_ctx* c, const uint64_t* psi_det, int64_t n_det) {
     c->have_dets = true;
     rc = qp_build_pairs(c);
   }
-  if (rc == 0) rc = qp_build_sigma_items(c, &c->items);
+  if (rc == 0 && !c->direct) rc = qp_build_sigma_items(c, &c->items);
   if (rc == 0) rc = qp_det_features(c);
   qp_mark(c, "sigma work items");
   qp_report_marks(c);
@@ -502,6 +514,7 @@ int qpgpu_connected_pairs(qpgpu_ctx* c, int64_t* n_pairs, int32_t* I, int32_t* J
   if (rc) return rc;
   if (!n_pairs) return QPGPU_ERR_ARG;
   Lock l(c->mu);
+  if (c->direct) return qpgpu_fail(c, QPGPU_ERR_STATE, "pairs are not stored (direct sigma)");
   *n_pairs = c->P;
   if (cap <= 0) return QPGPU_OK;
   if (cap < c->P || !I || !J || !cls || !phase || !exc || !hij)

@@ -218,7 +218,9 @@ int qp_det_features(qpgpu_ctx* c) {
   else
     k_det_features<2><<<gsz(c->N), 256, 0, c->stream>>>(c->tab, c->d_alpha, c->d_beta, c->d_rows, c->d_cols,
                                                         (float4*)c->d_detfeat, c->N);
-  k_row_coupling<<<gsz(c->N * 32), 256, 0, c->stream>>>(c->d_rowptr, c->d_val64, (float4*)c->d_detfeat, c->N);
+  // coupling feature from the stored elements (left at 0 with the direct sigma)
+  if (!c->direct)
+    k_row_coupling<<<gsz(c->N * 32), 256, 0, c->stream>>>(c->d_rowptr, c->d_val64, (float4*)c->d_detfeat, c->N);
   QP_CUDA(c, cudaGetLastError());
   return 0;
 }

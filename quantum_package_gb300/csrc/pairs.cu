@@ -11,7 +11,12 @@
 //
 // Two passes run the same deterministic traversal: the first counts hits per
 // row, the second writes them (column = bilinear position of J, FP64 and FP32
-// matrix elements).  Same-spin classes scan a column (row) with one thread per
+// matrix elements).  A third mode (direct sigma, for determinant sets whose
+// pairs do not fit in device memory) runs the traversal at every sigma call
+// and accumulates h_IJ u_J for the row each thread (classes A, B) or warp
+// (class C) owns: class A writes v, class B adds to it, class C adds its sum
+// and the diagonal term and writes s, so no pair is stored and no atomic is
+// needed.  Same-spin classes scan a column (row) with one thread per
 // determinant; the column's strings are staged in shared memory and read by
 // every thread of the block as broadcasts.  Class C gives one warp per row and
 // compacts hits with __ballot_sync, scanning either the columns of the beta
@@ -68,11 +73,34 @@ struct BuildArgs {
   int* s2col;
   float* s2val;
   int* err;  // set when a fill pass would write past its row's segment
+  // direct sigma (MODE_SIGMA): v, s = H u, S^2 u for the selected rows, u (N, nst)
+  const double* u;
+  double* v;
+  double* s;
+  const double* hdiag;
+  const double* sdiag;
+  int nst;
+  int row_lo, row_hi, row_first, row_step;
 };
 
+constexpr int MODE_COUNT = 0, MODE_FILL = 1, MODE_SIGMA = 2;
+
+__device__ __forceinline__ bool dsel(const BuildArgs& a, int64_t k) {
+  return k >= a.row_lo && k < a.row_hi && ((k - a.row_first) % a.row_step) == 0;
+}
+
+// acc[st] += h * u[j][st]
+__device__ __forceinline__ void dacc(const BuildArgs& a, double h, int64_t j, double (&acc)[8]) {
+  const double* uj = a.u + j * a.nst;
+#pragma unroll
+  for (int st = 0; st < 8; ++st)
+    if (st < a.nst) acc[st] = fma(h, __ldg(uj + st), acc[st]);
+}
+
 // ---- class A: same beta column, alpha singles / doubles -------------------
-template <int NINT, bool FILL>
+template <int NINT, int MODE>
 __global__ void __launch_bounds__(BLK) k_class_a(BuildArgs a) {
+  constexpr bool FILL = MODE == MODE_FILL, SIG = MODE == MODE_SIGMA;
   __shared__ u64 tile[TILE * NINT];
   const int64_t r0 = (int64_t)blockIdx.x * BLK;
   if (r0 >= a.N) return;
@@ -97,6 +125,8 @@ __global__ void __launch_bounds__(BLK) k_class_a(BuildArgs a) {
     if (FILL) out = a.rowptr[k];
   }
   int cnt = 0;
+  double acc[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+  const bool act = valid && (!SIG || dsel(a, k));
   for (int t0 = U0; t0 < U1; t0 += TILE) {
     const int tn = min(TILE, U1 - t0);
     __syncthreads();
@@ -106,7 +136,7 @@ __global__ void __launch_bounds__(BLK) k_class_a(BuildArgs a) {
       for (int w = 0; w < NINT; ++w) tile[i * NINT + w] = a.alpha[(int64_t)ai * NINT + w];
     }
     __syncthreads();
-    if (valid) {
+    if (act) {
       const int lo = max(cs, t0), hi = min(ce, t0 + tn);
       for (int pos = lo; pos < hi; ++pos) {
         const u64* c = &tile[(pos - t0) * NINT];
@@ -114,7 +144,7 @@ __global__ void __launch_bounds__(BLK) k_class_a(BuildArgs a) {
 #pragma unroll
         for (int w = 0; w < NINT; ++w) d += popc64(my[w] ^ c[w]);
         if (d == 2 || d == 4) {
-          if (FILL) {
+          if (FILL || SIG) {
             u64 J[2 * NINT];
 #pragma unroll
             for (int w = 0; w < NINT; ++w) {
@@ -123,7 +153,9 @@ __global__ void __launch_bounds__(BLK) k_class_a(BuildArgs a) {
             }
             double v = (d == 2) ? h_mono_spin<NINT>(a.t, my, J, 1, nullptr, nullptr)
                                 : h_double_spin<NINT>(a.t, my, c, nullptr, nullptr);
-            if (cnt < a.cntA[k]) {
+            if (SIG) {
+              dacc(a, v, pos, acc);
+            } else if (cnt < a.cntA[k]) {
               a.colidx[out + cnt] = pos;
               a.val64[out + cnt] = v;
               a.val32[out + cnt] = (float)v;
@@ -136,12 +168,15 @@ __global__ void __launch_bounds__(BLK) k_class_a(BuildArgs a) {
       }
     }
   }
-  if (!FILL && valid) a.cntA[k] = cnt;
+  if (MODE == MODE_COUNT && valid) a.cntA[k] = cnt;
+  if (SIG && act)
+    for (int st = 0; st < a.nst; ++st) a.v[k * a.nst + st] = acc[st];
 }
 
 // ---- class B: same alpha row, beta singles / doubles ----------------------
-template <int NINT, bool FILL>
+template <int NINT, int MODE>
 __global__ void __launch_bounds__(BLK) k_class_b(BuildArgs a) {
+  constexpr bool FILL = MODE == MODE_FILL, SIG = MODE == MODE_SIGMA;
   __shared__ u64 tile[TILE * NINT];
   const int64_t q0 = (int64_t)blockIdx.x * BLK;
   if (q0 >= a.N) return;
@@ -166,6 +201,8 @@ __global__ void __launch_bounds__(BLK) k_class_b(BuildArgs a) {
     if (FILL) out = a.rowptr[k] + a.cntA[k];
   }
   int cnt = 0;
+  double acc[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+  const bool act = valid && (!SIG || dsel(a, k));
   for (int t0 = V0; t0 < V1; t0 += TILE) {
     const int tn = min(TILE, V1 - t0);
     __syncthreads();
@@ -175,7 +212,7 @@ __global__ void __launch_bounds__(BLK) k_class_b(BuildArgs a) {
       for (int w = 0; w < NINT; ++w) tile[i * NINT + w] = a.beta[(int64_t)bi * NINT + w];
     }
     __syncthreads();
-    if (valid) {
+    if (act) {
       const int lo = max(rs, t0), hi = min(re, t0 + tn);
       for (int pos = lo; pos < hi; ++pos) {
         const u64* c = &tile[(pos - t0) * NINT];
@@ -183,7 +220,7 @@ __global__ void __launch_bounds__(BLK) k_class_b(BuildArgs a) {
 #pragma unroll
         for (int w = 0; w < NINT; ++w) d += popc64(my[NINT + w] ^ c[w]);
         if (d == 2 || d == 4) {
-          if (FILL) {
+          if (FILL || SIG) {
             u64 J[2 * NINT];
 #pragma unroll
             for (int w = 0; w < NINT; ++w) {
@@ -192,7 +229,9 @@ __global__ void __launch_bounds__(BLK) k_class_b(BuildArgs a) {
             }
             double v = (d == 2) ? h_mono_spin<NINT>(a.t, my, J, 2, nullptr, nullptr)
                                 : h_double_spin<NINT>(a.t, my + NINT, c, nullptr, nullptr);
-            if (cnt < a.cntB[k]) {
+            if (SIG) {
+              dacc(a, v, a.t_order[pos], acc);
+            } else if (cnt < a.cntB[k]) {
               a.colidx[out + cnt] = a.t_order[pos];
               a.val64[out + cnt] = v;
               a.val32[out + cnt] = (float)v;
@@ -205,7 +244,9 @@ __global__ void __launch_bounds__(BLK) k_class_b(BuildArgs a) {
       }
     }
   }
-  if (!FILL && valid) a.cntB[k] = cnt;
+  if (MODE == MODE_COUNT && valid) a.cntB[k] = cnt;
+  if (SIG && act)
+    for (int st = 0; st < a.nst; ++st) a.v[k * a.nst + st] += acc[st];
 }
 
 // spin flip test of an alpha-single x beta-single pair: the two excitations
@@ -223,14 +264,17 @@ __device__ __forceinline__ bool spin_flip(const u64* my, const u64* ca, const u6
 }
 
 // ---- class C: alpha single x beta single, one warp per row ----------------
-template <int NINT, bool FILL>
+template <int NINT, int MODE>
 __global__ void __launch_bounds__(BLK) k_class_c(BuildArgs a) {
+  constexpr bool FILL = MODE == MODE_FILL, SIG = MODE == MODE_SIGMA;
   const int lane = threadIdx.x & 31;
   const int64_t warp = ((int64_t)blockIdx.x * BLK + threadIdx.x) >> 5;
   const int64_t nwarp = ((int64_t)gridDim.x * BLK) >> 5;
   const unsigned lt = (1u << lane) - 1u;
   for (int64_t k = warp; k < a.N; k += nwarp) {
+    if (SIG && !dsel(a, k)) continue;
     const int ai = a.rows[k], bi = a.cols[k];
+    double acc[8] = {0, 0, 0, 0, 0, 0, 0, 0}, sacc[8] = {0, 0, 0, 0, 0, 0, 0, 0};
     u64 my[2 * NINT];
 #pragma unroll
     for (int w = 0; w < NINT; ++w) {
@@ -268,6 +312,18 @@ __global__ void __launch_bounds__(BLK) k_class_c(BuildArgs a) {
           const unsigned bal = __ballot_sync(0xffffffffu, hit);
           const bool flip = hit && spin_flip<NINT>(my, ca, cb);
           const unsigned sbal = __ballot_sync(0xffffffffu, flip);
+          if (SIG && hit) {
+            u64 J[2 * NINT];
+#pragma unroll
+            for (int w = 0; w < NINT; ++w) {
+              J[w] = ca[w];
+              J[NINT + w] = cb[w];
+            }
+            double s2;
+            const double v = h_double_ab<NINT>(a.t, my, J, &s2, nullptr, nullptr);
+            dacc(a, v, pos, acc);
+            if (flip) dacc(a, s2, pos, sacc);
+          }
           if (FILL && hit) {
             u64 J[2 * NINT];
 #pragma unroll
@@ -323,6 +379,18 @@ __global__ void __launch_bounds__(BLK) k_class_c(BuildArgs a) {
           const unsigned bal = __ballot_sync(0xffffffffu, hit);
           const bool flip = hit && spin_flip<NINT>(my, ca, cb);
           const unsigned sbal = __ballot_sync(0xffffffffu, flip);
+          if (SIG && hit) {
+            u64 J[2 * NINT];
+#pragma unroll
+            for (int w = 0; w < NINT; ++w) {
+              J[w] = ca[w];
+              J[NINT + w] = cb[w];
+            }
+            double s2;
+            const double v = h_double_ab<NINT>(a.t, my, J, &s2, nullptr, nullptr);
+            dacc(a, v, a.t_order[q], acc);
+            if (flip) dacc(a, s2, a.t_order[q], sacc);
+          }
           if (FILL && hit) {
             u64 J[2 * NINT];
 #pragma unroll
@@ -356,9 +424,29 @@ __global__ void __launch_bounds__(BLK) k_class_c(BuildArgs a) {
         }
       }
     }
-    if (!FILL && lane == 0) {
+    if (MODE == MODE_COUNT && lane == 0) {
       a.cntC[k] = cnt;
       a.cntS[k] = scnt;
+    }
+    if (SIG) {
+      // lanes combined in a fixed butterfly order; lane 0 finishes the row
+#pragma unroll
+      for (int st = 0; st < 8; ++st) {
+        if (st >= a.nst) break;
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+          acc[st] += __shfl_xor_sync(0xffffffffu, acc[st], o);
+          sacc[st] += __shfl_xor_sync(0xffffffffu, sacc[st], o);
+        }
+      }
+      if (lane == 0) {
+        const double hd = a.hdiag[k], sd = a.sdiag[k];
+        for (int st = 0; st < a.nst; ++st) {
+          const double uk = a.u[k * a.nst + st];
+          a.v[k * a.nst + st] = (a.v[k * a.nst + st] + acc[st]) + hd * uk;
+          a.s[k * a.nst + st] = sacc[st] + sd * uk;
+        }
+      }
     }
   }
 }
@@ -391,13 +479,10 @@ __global__ void k_diag(DevTables t, const u64* alpha, const u64* beta, const int
   }
 }
 
-template <int NINT>
-int build_pairs_t(qpgpu_ctx* c) {
-  const int64_t N = c->N;
-  cudaStream_t st = c->stream;
+BuildArgs index_args(const qpgpu_ctx* c) {
   BuildArgs a{};
   a.t = c->tab;
-  a.N = N;
+  a.N = c->N;
   a.alpha = c->d_alpha;
   a.beta = c->d_beta;
   a.rows = c->d_rows;
@@ -412,6 +497,18 @@ int build_pairs_t(qpgpu_ctx* c) {
   a.sb_idx = c->d_sb_idx;
   a.cost_a = c->d_cost_a;
   a.cost_b = c->d_cost_b;
+  a.row_lo = 0;
+  a.row_hi = (int)c->N;
+  a.row_first = 0;
+  a.row_step = 1;
+  return a;
+}
+
+template <int NINT>
+int build_pairs_t(qpgpu_ctx* c) {
+  const int64_t N = c->N;
+  cudaStream_t st = c->stream;
+  BuildArgs a = index_args(c);
   Scoped<int> cA, cB, cC, cS;
   QP_CUDA(c, dev_alloc(&cA.p, N));
   QP_CUDA(c, dev_alloc(&cB.p, N));
@@ -424,11 +521,11 @@ int build_pairs_t(qpgpu_ctx* c) {
   const unsigned gAB = nblocks(N, BLK);
   const unsigned gC = nblocks(N * 32, BLK);
   qp_mark(c, "pair setup");
-  k_class_a<NINT, false><<<gAB, BLK, 0, st>>>(a);
+  k_class_a<NINT, MODE_COUNT><<<gAB, BLK, 0, st>>>(a);
   qp_mark(c, "count A (same beta)");
-  k_class_b<NINT, false><<<gAB, BLK, 0, st>>>(a);
+  k_class_b<NINT, MODE_COUNT><<<gAB, BLK, 0, st>>>(a);
   qp_mark(c, "count B (same alpha)");
-  k_class_c<NINT, false><<<gC, BLK, 0, st>>>(a);
+  k_class_c<NINT, MODE_COUNT><<<gC, BLK, 0, st>>>(a);
   qp_mark(c, "count C (alpha x beta)");
   QP_CUDA(c, cudaGetLastError());
   Scoped<int64_t> tot, stot;
@@ -447,6 +544,28 @@ int build_pairs_t(qpgpu_ctx* c) {
   QP_CUDA(c, cudaMemcpyAsync(&c->P_s2, c->d_s2ptr + N, sizeof(int64_t), cudaMemcpyDeviceToHost, st));
   QP_CUDA(c, cudaStreamSynchronize(st));
   const int64_t P = c->P, PS = c->P_s2;
+  // stored pairs (16 B each, S^2 pairs 8 B) or the direct sigma: forced by
+  // qpgpu_set_sigma_mode, else direct when the stored pairs would leave less
+  // than 1/16 of the device memory free
+  bool direct = c->sigma_mode == QPGPU_SIGMA_DIRECT;
+  if (c->sigma_mode == QPGPU_SIGMA_AUTO) {
+    size_t fr = 0, total = 0;
+    QP_CUDA(c, cudaMemGetInfo(&fr, &total));
+    const double need = 16.0 * (double)P + 8.0 * (double)PS + 28.0 * (double)N;
+    direct = need + (double)total / 16.0 > (double)fr;
+  }
+  c->direct = direct;
+  if (direct) {
+    QP_CUDA(c, dev_alloc(&c->d_hdiag, N));
+    QP_CUDA(c, dev_alloc(&c->d_sdiag, N));
+    QP_CUDA(c, dev_alloc(&c->d_hdiag32, N));
+    k_diag<NINT><<<nblocks(N, 256), 256, 0, st>>>(c->tab, c->d_alpha, c->d_beta, c->d_rows, c->d_cols, c->d_hdiag,
+                                                   c->d_sdiag, c->d_hdiag32, N);
+    qp_mark(c, "diagonal (direct sigma: no pairs stored)");
+    QP_CUDA(c, cudaGetLastError());
+    QP_CUDA(c, cudaStreamSynchronize(st));
+    return 0;
+  }
   if (dev_alloc(&c->d_colidx, P) != cudaSuccess || dev_alloc(&c->d_val64, P) != cudaSuccess ||
       dev_alloc(&c->d_val32, P) != cudaSuccess || dev_alloc(&c->d_s2col, PS) != cudaSuccess ||
       dev_alloc(&c->d_s2val, PS) != cudaSuccess) {
@@ -466,11 +585,11 @@ int build_pairs_t(qpgpu_ctx* c) {
   QP_CUDA(c, cudaMemsetAsync(err.p, 0, sizeof(int), st));
   a.err = err.p;
   qp_mark(c, "scan + alloc");
-  k_class_a<NINT, true><<<gAB, BLK, 0, st>>>(a);
+  k_class_a<NINT, MODE_FILL><<<gAB, BLK, 0, st>>>(a);
   qp_mark(c, "fill A");
-  k_class_b<NINT, true><<<gAB, BLK, 0, st>>>(a);
+  k_class_b<NINT, MODE_FILL><<<gAB, BLK, 0, st>>>(a);
   qp_mark(c, "fill B");
-  k_class_c<NINT, true><<<gC, BLK, 0, st>>>(a);
+  k_class_c<NINT, MODE_FILL><<<gC, BLK, 0, st>>>(a);
   qp_mark(c, "fill C");
   QP_CUDA(c, cudaGetLastError());
   int herr = 0;
@@ -488,7 +607,42 @@ int build_pairs_t(qpgpu_ctx* c) {
   return 0;
 }
 
+template <int NINT>
+void sigma_direct_t(qpgpu_ctx* c, double* v, double* s, const double* u, int nst, cudaStream_t st, int row_lo,
+                    int row_hi, int row_first, int row_step) {
+  BuildArgs a = index_args(c);
+  a.u = u;
+  a.v = v;
+  a.s = s;
+  a.hdiag = c->d_hdiag;
+  a.sdiag = c->d_sdiag;
+  a.nst = nst;
+  a.row_lo = row_lo;
+  a.row_hi = row_hi;
+  a.row_first = row_first;
+  a.row_step = row_step;
+  const unsigned gAB = nblocks(c->N, BLK);
+  const unsigned gC = nblocks(c->N * 32, BLK);
+  k_class_a<NINT, MODE_SIGMA><<<gAB, BLK, 0, st>>>(a);
+  k_class_b<NINT, MODE_SIGMA><<<gAB, BLK, 0, st>>>(a);
+  k_class_c<NINT, MODE_SIGMA><<<gC, BLK, 0, st>>>(a);
+}
+
 }  // namespace
+
+// Direct sigma (FP64, nothing stored): v, s of the rows selected by (row_lo,
+// row_hi, row_first, row_step), bilinear order, u (N, nst).
+int qp_sigma_direct(qpgpu_ctx* c, double* v, double* s, const double* u, int nst, cudaStream_t st, int row_lo,
+                    int row_hi, int row_first, int row_step) {
+  if (nst < 1 || nst > 8) return qpgpu_fail(c, QPGPU_ERR_ARG, "n_st must be in 1..8 per sigma block");
+  if (row_step < 1) return qpgpu_fail(c, QPGPU_ERR_ARG, "row step must be >= 1");
+  if (c->nint == 1)
+    sigma_direct_t<1>(c, v, s, u, nst, st, row_lo, row_hi, row_first, row_step);
+  else
+    sigma_direct_t<2>(c, v, s, u, nst, st, row_lo, row_hi, row_first, row_step);
+  QP_CUDA(c, cudaGetLastError());
+  return 0;
+}
 
 void qp_free_pairs(qpgpu_ctx* c) {
   void** ps[] = {(void**)&c->d_rowptr, (void**)&c->d_colidx, (void**)&c->d_val64, (void**)&c->d_val32,
@@ -499,6 +653,7 @@ void qp_free_pairs(qpgpu_ctx* c) {
     *p = nullptr;
   }
   c->have_pairs = false;
+  c->direct = false;
   c->P = c->P_s2 = 0;
 }
 

@@ -393,6 +393,8 @@ struct qpgpu_ctx {
 
   // Hamiltonian in CSR over bilinear rows (columns are bilinear positions)
   bool have_pairs = false;
+  int sigma_mode = QPGPU_SIGMA_AUTO;  // qpgpu_set_sigma_mode
+  bool direct = false;                // pairs not stored: sigma enumerates them (pairs.cu)
   int64_t P = 0;
   int64_t* d_rowptr = nullptr;  // N+1
   int* d_colidx = nullptr;      // P
@@ -443,6 +445,9 @@ int qp_build_pairs(qpgpu_ctx* c);      // pairs.cu
 void qp_free_dets(qpgpu_ctx* c);       // index.cu
 void qp_free_pairs(qpgpu_ctx* c);      // pairs.cu
 int qp_build_sigma_items(qpgpu_ctx* c, SigmaItems* it);  // sigma.cu
+// FP64 sigma without stored pairs (pairs.cu)
+int qp_sigma_direct(qpgpu_ctx* c, double* v, double* s, const double* u, int nst, cudaStream_t st, int row_lo,
+                    int row_hi, int row_first, int row_step);
 // u32_ld: floats between FP32 rows (0: n_st; or n_st padded by qp_pad_states)
 int qp_sigma_launch(qpgpu_ctx* c, SigmaItems* it, double* v, double* s, const double* u, const float* u32, int nst,
                     int precision, cudaStream_t st, int row_lo, int row_hi, int row_first, int row_step,

@@ -475,6 +475,7 @@ int qp_sigma_launch(qpgpu_ctx* c, SigmaItems* it, double* v, double* s, const do
                     int precision, cudaStream_t st, int row_lo, int row_hi, int row_first, int row_step,
                     int u32_ld) {
   if (nst < 1 || nst > 8) return qpgpu_fail(c, QPGPU_ERR_ARG, "n_st must be in 1..8 per sigma block");
+  if (c->direct) return qp_sigma_direct(c, v, s, u, nst, st, row_lo, row_hi, row_first, row_step);
   if (u32_ld <= 0) u32_ld = nst;
   if (u32_ld != nst && !(u32_ld == qp_pad_states(nst) && (((uintptr_t)u32) & 31) == 0))
     return qpgpu_fail(c, QPGPU_ERR_ARG, "FP32 rows must be n_st floats apart, or padded to 4/8 and 32-byte aligned");
@@ -561,6 +562,7 @@ extern "C" int qpgpu_sigma_bilinear_noalloc(qpgpu_ctx* c, double* v_t, double* s
                                             const float* u_t32, int n_st, int precision, void* stream) {
   if (!c) return QPGPU_ERR_ARG;
   if (!c->have_ints || !c->have_pairs) return qpgpu_fail(c, QPGPU_ERR_STATE, "determinants not set");
+  if (c->direct) return qpgpu_fail(c, QPGPU_ERR_STATE, "the no-alloc sigma needs stored pairs (direct sigma set)");
   if (!v_t || !s_t || !u_t || n_st < 1 || n_st > 8 || (precision != QPGPU_FP64 && precision != QPGPU_FP32) ||
       (precision == QPGPU_FP32 && !u_t32))
     return qpgpu_fail(c, QPGPU_ERR_ARG, "bad sigma arguments (n_st must be 1..8)");

@@ -37,7 +37,7 @@ def stream_handle(stream):
 class Wavefunction:
     """Providers of one orbital space and determinant set, on the GPU."""
 
-    def __init__(self, n_mo: int, n_alpha: int, n_beta: int, h=None, eri=None, psi_det=None):
+    def __init__(self, n_mo: int, n_alpha: int, n_beta: int, h=None, eri=None, psi_det=None, sigma_mode=0):
         L = _lib.load()
         self.n_mo, self.n_alpha, self.n_beta = n_mo, n_alpha, n_beta
         self.n_int = (n_mo - 1) // 64 + 1
@@ -47,14 +47,20 @@ class Wavefunction:
             raise _lib.QPGPUError(rc, "qpgpu_create failed (device or arguments)")
         self._ctx = h_
         self.n_det = 0
+        if sigma_mode:
+            self.set_sigma_mode(sigma_mode)
         if h is not None:
             self.set_integrals(h, eri)
         if psi_det is not None:
             self.set_dets(psi_det)
 
     @classmethod
-    def from_problem(cls, prob):
-        return cls(prob.n_mo, prob.n_alpha, prob.n_beta, prob.ints.h, prob.ints.eri, prob.dets)
+    def from_problem(cls, prob, sigma_mode=0):
+        return cls(prob.n_mo, prob.n_alpha, prob.n_beta, prob.ints.h, prob.ints.eri, prob.dets, sigma_mode)
+
+    def set_sigma_mode(self, mode):
+        """SIGMA_AUTO (0), SIGMA_STORED (1) or SIGMA_DIRECT (2); takes effect at the next set_dets."""
+        check(_lib.load().qpgpu_set_sigma_mode(self._ctx, int(mode)), self._ctx)
 
     def close(self):
         if getattr(self, "_ctx", None):
