@@ -236,6 +236,9 @@ def davidson_block(prob, wf):
     u = _guess(N, prob.seed)
     kw = dict(n_states=N_STATES, s2_eig=False, max_iter=400, davidson_sze_max=SZE_MAX)
     tight = wf.davidson_diag_hs2(u, threshold=1e-12, **kw)
+    # one-time costs of the FP32 path (module load, launch-shape tuning for this
+    # determinant set) outside the timed runs, as the set-up is
+    wf.davidson_diag_hs2(u, threshold=1e-10, precision=FP32, **dict(kw, max_iter=3))
     e_ref = tight["energies"][:N_STATES]
     out = {"n_states": N_STATES, "n_states_diag": N_STATES_DIAG, "davidson_sze_max": SZE_MAX,
            "threshold": 1e-10, "e_tol_ha": E_TOL,
@@ -267,6 +270,7 @@ def davidson_block(prob, wf):
         loss = wf.mlp_train(epochs=20, batch=4096, lr=2e-3, seed=4)
         train[str(n_stage)] = {"n_sigma": r["n_sigma"], "samples": int(r["n_samples"]), "loss": loss}
     wf.set_dets(prob.dets)
+    wf.davidson_diag_hs2(u, threshold=1e-10, precision=FP32, **dict(kw, max_iter=3))  # tuning, as above
     out["training"] = {"stages": train, "wall_s": time.perf_counter() - t0,
                        "note": "training on earlier determinant sets; not part of time-to-E"}
     # learned step in place of the diagonal step (preconditioner=1), and as an

@@ -84,6 +84,14 @@ int qpgpu_get_info(qpgpu_ctx* ctx, qpgpu_info* info);
 #define QPGPU_SIGMA_DIRECT 2
 int qpgpu_set_sigma_mode(qpgpu_ctx* ctx, int mode);
 
+/* u_0_H_u_0 (src/Davidson/diagonalization_hs2.irp.f:446-484), the psi_energy
+ * provider's routine: e_0[i] = <u_0(:,i)|H|u_0(:,i)> over the N_det rows of the
+ * host array u_0(ld, n_st) (column-major, psi_det order), FP64 sigma on the
+ * device.  As in the reference the value is not divided by <u|u> (psi_coef is
+ * normalised) and a zero column gives 0; electronic energy (no nuclear
+ * repulsion). */
+int qpgpu_u0_h_u0(qpgpu_ctx* ctx, double* e_0, const double* u_0, int n_st, int64_t ld);
+
 /* Integrals (host).  h_pq: n_mo x n_mo column-major, symmetric
  * (mo_mono_elec_integral, src/Integrals_Monoelec/mo_mono_ints.irp.f:1-26).
  * eri_packed: chemist (pq|rs) at bielec_integrals_index key - 1

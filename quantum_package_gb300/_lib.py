@@ -82,6 +82,7 @@ def load():
         "qpgpu_last_error": (C.c_char_p, [vp]),
         "qpgpu_get_info": (C.c_int, [vp, C.POINTER(Info)]),
         "qpgpu_set_sigma_mode": (C.c_int, [vp, C.c_int]),
+        "qpgpu_u0_h_u0": (C.c_int, [vp, vp, vp, C.c_int, C.c_int64]),
         "qpgpu_set_integrals": (C.c_int, [vp, vp, vp]),
         "qpgpu_set_dets": (C.c_int, [vp, vp, C.c_int64]),
         "qpgpu_h_s2_u0": (C.c_int, [vp, vp, vp, vp, C.c_int, C.c_int64]),

@@ -445,6 +445,86 @@ int qpgpu_h_s2_u0(qpgpu_ctx* c, double* v0, double* s0, const double* u0, int n_
   return rc;
 }
 
+namespace {
+constexpr int DOT_CTA = 256, DOT_GRID = 2 * 152;
+// per-CTA partial sums of u.u and u.v for each column (fixed summation order)
+__global__ void k_col_dots(const double* u, const double* v, int64_t N, int n_st, double* partial) {
+  __shared__ double red[2][DOT_CTA / 32];
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  for (int i = 0; i < n_st; ++i) {
+    const double* ui = u + (int64_t)i * N;
+    const double* vi = v + (int64_t)i * N;
+    double uu = 0.0, uv = 0.0;
+    for (int64_t r = blockIdx.x * (int64_t)DOT_CTA + threadIdx.x; r < N; r += (int64_t)gridDim.x * DOT_CTA) {
+      uu = fma(ui[r], ui[r], uu);
+      uv = fma(ui[r], vi[r], uv);
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+      uu += __shfl_xor_sync(0xffffffffu, uu, o);
+      uv += __shfl_xor_sync(0xffffffffu, uv, o);
+    }
+    if (lane == 0) {
+      red[0][w] = uu;
+      red[1][w] = uv;
+    }
+    __syncthreads();
+    if (threadIdx.x < 2) {
+      double t = 0.0;
+      for (int q = 0; q < DOT_CTA / 32; ++q) t += red[threadIdx.x][q];
+      partial[((int64_t)blockIdx.x * n_st + i) * 2 + threadIdx.x] = t;
+    }
+    __syncthreads();
+  }
+}
+}  // namespace
+
+int qpgpu_u0_h_u0(qpgpu_ctx* c, double* e_0, const double* u0, int n_st, int64_t ld) {
+  int rc = check_ctx(c, true, true);
+  if (rc) return rc;
+  if (!e_0 || !u0 || n_st < 1 || ld < c->N) return qpgpu_fail(c, QPGPU_ERR_ARG, "bad u_0_H_u_0 arguments");
+  const int64_t N = c->N;
+  const size_t cols = (size_t)N * n_st;
+  {
+    Lock l(c->mu);
+    if (c->stage_bytes < 3 * cols * sizeof(double)) {
+      dev_free(c->d_stage);
+      c->d_stage = nullptr;
+      c->stage_bytes = 0;
+      QP_CUDA(c, cudaMalloc((void**)&c->d_stage, 3 * cols * sizeof(double)));
+      c->stage_bytes = 3 * cols * sizeof(double);
+    }
+  }
+  double *du = c->d_stage, *dv = du + cols, *ds = du + 2 * cols;
+  cudaStream_t st = c->stream;
+  double* dpart = nullptr;
+  QP_CUDA(c, cudaMalloc((void**)&dpart, (size_t)DOT_GRID * n_st * 2 * sizeof(double)));
+  std::vector<double> part((size_t)DOT_GRID * n_st * 2);
+  if (cudaMemcpy2DAsync(du, N * sizeof(double), u0, ld * sizeof(double), N * sizeof(double), n_st,
+                        cudaMemcpyHostToDevice, st) != cudaSuccess)
+    rc = qpgpu_fail(c, QPGPU_ERR_CUDA, "copy of u_0 failed");
+  if (!rc) rc = qpgpu_h_s2_u0_device(c, dv, ds, du, n_st, N, QPGPU_FP64, st);
+  if (!rc) {
+    k_col_dots<<<DOT_GRID, DOT_CTA, 0, st>>>(du, dv, N, n_st, dpart);
+    if (cudaMemcpyAsync(part.data(), dpart, part.size() * sizeof(double), cudaMemcpyDeviceToHost, st) !=
+        cudaSuccess)
+      rc = qpgpu_fail(c, QPGPU_ERR_CUDA, "copy of the dot products failed");
+  }
+  const cudaError_t e = cudaStreamSynchronize(st);
+  cudaFree(dpart);
+  if (!rc && e != cudaSuccess) rc = qpgpu_fail(c, QPGPU_ERR_CUDA, cudaGetErrorString(e));
+  if (rc) return rc;
+  for (int i = 0; i < n_st; ++i) {
+    double uu = 0.0, uv = 0.0;
+    for (int q = 0; q < DOT_GRID; ++q) {
+      uu += part[((size_t)q * n_st + i) * 2];
+      uv += part[((size_t)q * n_st + i) * 2 + 1];
+    }
+    e_0[i] = (uu != 0.0) ? uv : 0.0;  // the reference's test on u_dot_u; no division (:470-477)
+  }
+  return QPGPU_OK;
+}
+
 int qpgpu_h_s2_u0_work(qpgpu_ctx* c, double* v_t, double* s_t, const double* u_t, int n_st, int istart, int iend,
                        int ishift, int istep) {
   int rc = check_ctx(c, true, true);

@@ -94,6 +94,14 @@ class Wavefunction:
         check(_lib.load().qpgpu_get_info(self._ctx, C.byref(i)), self._ctx)
         return {f: getattr(i, f) for f, _ in i._fields_}
 
+    def u_0_H_u_0(self, u_0):
+        """e_0[i] = <u_0[i]|H|u_0[i]> (not divided by the norm, as the reference); u_0: (N_st, sze)."""
+        u = np.ascontiguousarray(np.atleast_2d(u_0), dtype=np.float64)
+        n_st, ld = u.shape
+        e = np.zeros(n_st)
+        check(_lib.load().qpgpu_u0_h_u0(self._ctx, _p(e), _p(u), n_st, ld), self._ctx)
+        return e
+
     # --- sigma ---------------------------------------------------------
     def H_S2_u_0_nstates_openmp(self, u_0):
         """v_0 = H u_0, s_0 = S^2 u_0 (no S_z(S_z-1) shift); u_0: (N_st, sze) -> (v_0, s_0)."""

@@ -171,3 +171,16 @@ def test_invalid_inputs_raise():
     bad[0, 1, 0] = np.uint64((1 << 12) | 3)  # orbital 13 > n_mo
     with pytest.raises(QPGPUError):
         wf.set_dets(bad)
+
+
+def test_u0_h_u0_matches_oracle():
+    # u_0_H_u_0 (diagonalization_hs2.irp.f:446-484): <u|H|u> per column, not
+    # divided by <u|u>; a zero column gives 0
+    p, o, wf = _problem(2, n_det=5_000)
+    u = G.random_coefficients(p.n_det, 3, p.seed)
+    u[1] = 0.0
+    e = wf.u_0_H_u_0(u)
+    v, _ = o.h_s2_u0(u)
+    ref = np.einsum("ij,ij->i", u, v)
+    assert e[1] == 0.0
+    np.testing.assert_allclose(e[[0, 2]], ref[[0, 2]], rtol=REL64, atol=0)
