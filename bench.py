@@ -382,6 +382,12 @@ def run_ours(args):
     stored_bytes = P * (4 + 8) + N * N_STATES * 8 * 3 + N * 28
     achieved = alg_bytes / (ms64 * 1e-3) / 1e9
     traffic, tnote = profiled_traffic(N, P)
+    fp64_pipe = None
+    try:
+        with open(os.path.join(ROOT, "profiles", "sigma_fp64_ncu.json")) as f:
+            fp64_pipe = json.load(f).get("fp64_pipe_active")
+    except (OSError, ValueError):
+        pass
     value = world * N * N_STATES / (ms64 * 1e-3)
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
@@ -396,6 +402,9 @@ def run_ours(args):
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": achieved / peak, "traffic": traffic, "peak_kind": peak_kind,
                      "kernel": "k_sigma64<4>",
+                     "fp64_pipe_active": fp64_pipe,
+                     "bound_note": "the HBM fraction is reported as the contract asks; ncu shows the FP64 pipe "
+                                   "(about 2 FMA/clk/SM on GB300) as the limiting unit (fp64_pipe_active)",
                      "algorithmic_bytes_per_launch": alg_bytes,
                      "stored_pair_bytes_per_launch": stored_bytes,
                      "stored_pair_frac": stored_bytes / (ms64 * 1e-3) / 1e9 / peak,
