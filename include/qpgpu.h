@@ -42,6 +42,11 @@ extern "C" {
 #define QPGPU_FP64 0  /* FP64 matrix elements and products */
 #define QPGPU_FP32 1  /* FP32 elements and products, Kahan-compensated per-row sums,
                          FP64 diagonal */
+#define QPGPU_FF 2    /* float-float (hi + lo FP32 pairs, about 47 significant bits) elements,
+                         coefficients and sums on the FP32 pipes, FP64 diagonal: FP64-class
+                         accuracy (1e-13 relative) at FP32-pipe speed.  No counterpart in the
+                         reference.  In qpgpu_davidson_hs2 it selects FP32 sigma with a
+                         float-float sigma as the restart (defect-correction) sigma. */
 
 typedef struct qpgpu_ctx qpgpu_ctx;
 

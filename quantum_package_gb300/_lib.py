@@ -16,7 +16,7 @@ ERRORS = {
     -1: "QPGPU_ERR_ARG", -2: "QPGPU_ERR_STATE", -3: "QPGPU_ERR_CUDA", -4: "QPGPU_ERR_NOMEM",
     -5: "QPGPU_ERR_DAVIDSON", -6: "QPGPU_ERR_TIMEOUT", -7: "QPGPU_ERR_NUMERIC",
 }
-FP64, FP32 = 0, 1
+FP64, FP32, FF = 0, 1, 2
 SIGMA_AUTO, SIGMA_STORED, SIGMA_DIRECT = 0, 1, 2  # qpgpu_set_sigma_mode
 
 HEADER = os.path.join(os.path.dirname(os.path.dirname(os.path.abspath(__file__))), "include", "qpgpu.h")

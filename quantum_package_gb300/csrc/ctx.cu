@@ -213,6 +213,7 @@ int qpgpu_destroy(qpgpu_ctx* c) {
     c->mlp.free_all();
     dev_free(c->d_work);
     dev_free(c->d_stage);
+    dev_free(c->d_ffu);
     cudaStreamDestroy(c->stream);
   }
   delete c;
@@ -375,12 +376,14 @@ int qpgpu_sigma_bilinear(qpgpu_ctx* c, double* v_t, double* s_t, const double* u
                          int precision, void* stream) {
   int rc = check_ctx(c, true, true);
   if (rc) return rc;
-  if (!v_t || !s_t || !u_t || n_st < 1 || n_st > 8 || (precision != QPGPU_FP64 && precision != QPGPU_FP32))
+  if (!v_t || !s_t || !u_t || n_st < 1 || n_st > 8 ||
+      (precision != QPGPU_FP64 && precision != QPGPU_FP32 && precision != QPGPU_FF))
     return qpgpu_fail(c, QPGPU_ERR_ARG, "bad sigma arguments (n_st must be 1..8)");
   if (((uintptr_t)u_t & 15) || (u_t32 && ((uintptr_t)u_t32 & 15)))
     return qpgpu_fail(c, QPGPU_ERR_ARG, "u_t and u_t32 must be 16-byte aligned");
   Lock l(c->mu);
   cudaStream_t st = stream ? (cudaStream_t)stream : c->stream;
+  if (precision == QPGPU_FF) return qp_sigma_ff(c, &c->items, v_t, s_t, u_t, n_st, st, 0, (int)c->N, 0, 1);
   return qp_sigma_launch(c, &c->items, v_t, s_t, u_t, u_t32, n_st, precision, st, 0, (int)c->N, 0, 1);
 }
 

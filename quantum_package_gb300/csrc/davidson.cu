@@ -19,7 +19,9 @@
 // the first iteration of each restart cycle, which runs the FP64 sigma on the
 // re-contracted Ritz vectors (defect correction).  Convergence is accepted only
 // on an FP64 iteration; an FP32 iteration that meets the threshold forces a
-// restart, so the reported energies and residuals are FP64 ones.
+// restart, so the reported energies and residuals are FP64 ones.  With
+// QPGPU_FF the restart sigma is the float-float one (k_sigma_ff, FP64-class
+// accuracy on the FP32 pipes) and convergence is accepted on those iterations.
 #include <algorithm>
 #include <cmath>
 #include <cstring>
@@ -307,35 +309,6 @@ __global__ void __launch_bounds__(DBLK) k_lincomb(LinComb L, int nb, int64_t N, 
   }
 }
 
-// Float-float (hi + lo) form of a double, built with integer and FP32
-// instructions only: hi keeps the top 24 bits of the significand
-// (truncated), lo the next 23 (the last 6 bits, below 2^-46 |x|, are
-// dropped), so hi + lo carries about 47 significant bits.  |x| below 2^-126
-// gives (0, 0) and below 2^-80 lo = 0, absolute errors far below anything a
-// Davidson vector resolves.  Finite |x| < 2^127 is assumed (normalised CI
-// vectors and their sigma).
-__device__ __forceinline__ void split_ff(double x, float& hi, float& lo) {
-  const unsigned long long b = (unsigned long long)__double_as_longlong(x);
-  const unsigned h32 = (unsigned)(b >> 32), l32 = (unsigned)b;
-  const unsigned sign = h32 & 0x80000000u;
-  const int e = (int)((h32 >> 20) & 0x7ffu);
-  const int fe = e - 896;  // float biased exponent of hi (e - 1023 + 127)
-  if (fe <= 0) {
-    hi = 0.f;
-    lo = 0.f;
-    return;
-  }
-  hi = __uint_as_float(sign | ((unsigned)fe << 23) | ((h32 & 0xfffffu) << 3) | (l32 >> 29));
-  const int se = e - 942;  // biased exponent of 2^(e - 1069)
-  if (se <= 0) {
-    lo = 0.f;
-    return;
-  }
-  const float r = __fsub_rn(__uint_as_float(0x4B000000u | ((l32 & 0x1fffffffu) >> 6)), 8388608.0f);
-  lo = __fmul_rn(r, __uint_as_float((unsigned)se << 23));
-  if (sign) lo = -lo;
-}
-
 // k_lincomb in float-float arithmetic on the FP32 pipes (GB300 issues 64
 // FP32 FMAs for each FP64 FMA): each product of split operands is formed
 // exactly for hi*hi (an FMA gives its rounding error) plus the hi*lo cross
@@ -349,7 +322,7 @@ __global__ void __launch_bounds__(DBLK) k_lincomb_ff(LinComb L, int nb, int64_t 
   __shared__ float2 Cs[MAXM * MAXS];
   for (int i = threadIdx.x; i < nb * NSD * NSD; i += DBLK) {
     float h, l;
-    split_ff(C[i], h, l);
+    qpsig::split_ff(C[i], h, l);
     Cs[i] = make_float2(h, l);
   }
   __syncthreads();
@@ -368,7 +341,7 @@ __global__ void __launch_bounds__(DBLK) k_lincomb_ff(LinComb L, int nb, int64_t 
 #pragma unroll
         for (int c = 0; c < NSD; ++c) {
           float xh, xl;
-          split_ff(x[c], xh, xl);
+          qpsig::split_ff(x[c], xh, xl);
 #pragma unroll
           for (int j = 0; j < NSD; ++j) {
             const float2 cv = cb[c * NSD + j];
@@ -916,14 +889,15 @@ extern "C" int qpgpu_davidson_hs2(qpgpu_ctx* c, double* u_in, int64_t dim_in, do
   const int64_t N = c->N;
   const int nst = prm->n_states, nsd = prm->n_states_diag;
   if (nst < 1 || nsd < nst || nsd > MAXS || dim_in < N || prm->davidson_sze_max < 1 ||
-      (prm->precision != QPGPU_FP64 && prm->precision != QPGPU_FP32))
+      (prm->precision != QPGPU_FP64 && prm->precision != QPGPU_FP32 && prm->precision != QPGPU_FF))
     return qpgpu_fail(c, QPGPU_ERR_ARG, "bad Davidson parameters (1 <= n_states <= n_states_diag <= 8)");
   if (prm->preconditioner < 0 || prm->preconditioner > 2)
     return qpgpu_fail(c, QPGPU_ERR_ARG, "preconditioner must be 0 (diagonal), 1 (learned) or 2 (learned, extra direction)");
   if ((int64_t)nsd * 3 > N) return qpgpu_fail(c, QPGPU_ERR_ARG, "N_st_diag*3 > sze (diagonalization_hs2.irp.f:110)");
   int itermax = std::max(3, (int)std::min<int64_t>(prm->davidson_sze_max, N / nsd));
   while (itermax * nsd > MAXM) --itermax;
-  const bool mixed = prm->precision == QPGPU_FP32;
+  const bool mixed = prm->precision == QPGPU_FP32 || prm->precision == QPGPU_FF;
+  const int restart_prec = prm->precision == QPGPU_FF ? QPGPU_FF : QPGPU_FP64;  // defect-correction sigma
   if (mixed && prm->defect_every > 0) itermax = std::max(3, std::min(itermax, prm->defect_every + 1));
   const int max_sigma = prm->max_iter > 0 ? prm->max_iter : 1000;
 
@@ -1019,10 +993,12 @@ extern "C" int qpgpu_davidson_hs2(qpgpu_ctx* c, double* u_in, int64_t dim_in, do
       orthonormalise(d, b);
       prof.mark(DavProf::ORTHO);
       // sigma on block b
-      const int prec = (mixed && iter > 1) ? QPGPU_FP32 : QPGPU_FP64;
+      const int prec = (mixed && iter > 1) ? QPGPU_FP32 : restart_prec;
       if (prec == QPGPU_FP32) qp_to_float(d.blk(d.U, b), d.u32, N, nsd, qp_pad_states(nsd), st);
-      int rc = qp_sigma_launch(c, &c->items, d.blk(d.W, b), d.blk(d.S, b), d.blk(d.U, b), d.u32, nsd, prec, st, 0,
-                               (int)N, 0, 1, qp_pad_states(nsd));
+      int rc = (prec == QPGPU_FF)
+                   ? qp_sigma_ff(c, &c->items, d.blk(d.W, b), d.blk(d.S, b), d.blk(d.U, b), nsd, st, 0, (int)N, 0, 1)
+                   : qp_sigma_launch(c, &c->items, d.blk(d.W, b), d.blk(d.S, b), d.blk(d.U, b), d.u32, nsd, prec, st,
+                                     0, (int)N, 0, 1, qp_pad_states(nsd));
       if (rc) return rc;
       ++n_sigma;
       prof.mark(DavProf::SIGMA);
@@ -1147,7 +1123,7 @@ extern "C" int qpgpu_davidson_hs2(qpgpu_ctx* c, double* u_in, int64_t dim_in, do
       if (failed) break;
       // davidson_converged, parameters.irp.f:9-49 ('residual'; not before the 2nd iteration)
       const bool below = std::fabs(mx) < prm->threshold;
-      if (below && prec == QPGPU_FP64 && (iter >= 2 || mixed)) {
+      if (below && prec != QPGPU_FP32 && (iter >= 2 || mixed)) {
         converged = true;
         break;
       }

@@ -646,6 +646,7 @@ int qp_sigma_direct(qpgpu_ctx* c, double* v, double* s, const double* u, int nst
 
 void qp_free_pairs(qpgpu_ctx* c) {
   void** ps[] = {(void**)&c->d_rowptr, (void**)&c->d_colidx, (void**)&c->d_val64, (void**)&c->d_val32,
+                 (void**)&c->d_val32lo,
                  (void**)&c->d_s2ptr, (void**)&c->d_s2col, (void**)&c->d_s2val, (void**)&c->d_hdiag,
                  (void**)&c->d_sdiag, (void**)&c->d_hdiag32};
   for (auto p : ps) {

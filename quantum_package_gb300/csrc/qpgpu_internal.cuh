@@ -400,6 +400,9 @@ struct qpgpu_ctx {
   int* d_colidx = nullptr;      // P
   double* d_val64 = nullptr;    // P
   float* d_val32 = nullptr;     // P
+  float* d_val32lo = nullptr;   // P, float-float sigma: val64 - val32 (built on first use)
+  float* d_ffu = nullptr;       // float-float sigma: (hi, lo) rows of the coefficients
+  size_t ffu_floats = 0;
   int64_t P_s2 = 0;             // alpha-beta spin-flip pairs (<I|S+S-|J> != 0)
   int64_t* d_s2ptr = nullptr;
   int* d_s2col = nullptr;
@@ -451,7 +454,11 @@ int qp_sigma_direct(qpgpu_ctx* c, double* v, double* s, const double* u, int nst
 // u32_ld: floats between FP32 rows (0: n_st; or n_st padded by qp_pad_states)
 int qp_sigma_launch(qpgpu_ctx* c, SigmaItems* it, double* v, double* s, const double* u, const float* u32, int nst,
                     int precision, cudaStream_t st, int row_lo, int row_hi, int row_first, int row_step,
-                    int u32_ld = 0);
+                    int u32_ld = 0, const float* u32lo = nullptr);
+// float-float sigma of an FP64 block u (N, nst): splits u and the stored
+// elements into FP32 pairs (scratch of the context) and runs k_sigma_ff
+int qp_sigma_ff(qpgpu_ctx* c, SigmaItems* it, double* v, double* s, const double* u, int nst, cudaStream_t st,
+                int row_lo, int row_hi, int row_first, int row_step);
 // FP32 row length that keeps a row of n_st coefficients in one 32-byte sector
 inline int qp_pad_states(int nst) { return nst <= 1 ? 1 : nst <= 2 ? 2 : nst <= 4 ? 4 : 8; }
 void qp_to_bilinear(const double* u0, int64_t ld, const int* order, double* ut, float* ut32, int nst, int64_t N,

@@ -36,6 +36,8 @@ struct SigArgs {
   const double* u;   // (N, NST) FP64
   const float* u32;  // (N, u32_ld) FP32 (precision FP32): rows u32_ld floats apart
   int u32_ld;
+  const float* u32lo;   // precision FF: low parts of u, same layout as u32 (the high parts)
+  const float* val32lo; // precision FF: low parts of the stored elements (val32 = high parts)
   double* v;
   double* s;
   double* pv;  // partial sums (n_items, NST)
@@ -303,6 +305,23 @@ __global__ void k_from_bilinear(const double* vt, int64_t ld, const int* order, 
 }
 
 // y (N rows of ld floats) <- x (N rows of nst doubles)
+// lo = val64 - val32 rounded to FP32 (the low parts of the stored elements)
+__global__ void k_lo_parts(const double* v64, const float* v32, float* lo, int64_t n) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+    lo[i] = (float)(v64[i] - (double)v32[i]);
+}
+
+// (hi, lo) rows of ld floats <- x (N rows of nst doubles), integer split
+__global__ void k_split_rows(const double* x, float* hi, float* lo, int64_t N, int nst, int ld) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < N * nst; i += (int64_t)gridDim.x * blockDim.x) {
+    float h, l;
+    split_ff(x[i], h, l);
+    const int64_t o = (i / nst) * ld + i % nst;
+    hi[o] = h;
+    lo[o] = l;
+  }
+}
+
 __global__ void k_to_float(const double* x, float* y, int64_t N, int nst, int ld) {
   for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < N * nst; i += (int64_t)gridDim.x * blockDim.x)
     y[(i / nst) * ld + i % nst] = (float)x[i];
@@ -366,9 +385,97 @@ void launch_sigma32(const SigArgs& a, int variant, cudaStream_t st, int n_sm) {
   if constexpr (NST != 8) launch_sigma32_ld<NST, NST, false>(a, variant, st, n_sm);
 }
 
+// Float-float sigma: elements h = vh + vl and coefficients u = uh + ul as
+// FP32 pairs (rows padded to LD floats, 32-byte aligned; LD = 8 uses one
+// 256-bit load per part).  Per pair and state the product is formed exactly
+// for vh*uh (FMA gives its rounding error) plus the cross terms, and each
+// lane keeps its sum as an unevaluated float pair updated with Knuth's
+// TwoSum; lanes are combined with reduce_scatter_ff.  About 1e-13 relative,
+// FP32 pipes only, except the FP64 diagonal term of the owner lanes.
+template <int NST, int LD>
+__global__ void __launch_bounds__(128) k_sigma_ff(SigArgs a) {
+  constexpr int NP = Pow2<NST>::v;
+  constexpr int UNRF = 2;
+  const int lane = threadIdx.x & 31;
+  const int64_t warp = ((int64_t)blockIdx.x * 128 + threadIdx.x) >> 5;
+  const int64_t nwarp = ((int64_t)gridDim.x * 128) >> 5;
+  for (int64_t it = warp; it < a.n_items; it += nwarp) {
+    const int k = a.item_row[it];
+    if (!row_selected(a, k)) continue;
+    const int j = a.item_sub[it];
+    const int64_t rb = a.rowptr[k], re = a.rowptr[k + 1];
+    const int64_t beg = rb + (int64_t)j * QP_SIGMA_CHUNK;
+    const int64_t end = min(beg + (int64_t)QP_SIGMA_CHUNK, re);
+    float ah[NP], al[NP];
+#pragma unroll
+    for (int st = 0; st < NP; ++st) ah[st] = al[st] = 0.f;
+    for (int64_t e0 = beg + lane; e0 < end; e0 += 32 * UNRF) {
+      int col[UNRF];
+      float vh[UNRF], vl[UNRF];
+#pragma unroll
+      for (int q = 0; q < UNRF; ++q) {
+        const int64_t e = e0 + 32 * q;
+        col[q] = e < end ? __ldg(&a.colidx[e]) : k;
+        vh[q] = e < end ? __ldg(&a.val32[e]) : 0.f;
+        vl[q] = e < end ? __ldg(&a.val32lo[e]) : 0.f;
+      }
+#pragma unroll
+      for (int q = 0; q < UNRF; ++q) {
+        float xh[NST], xl[NST];
+        load_row_ld<NST, LD, LD == 8>(a.u32, col[q], xh);
+        load_row_ld<NST, LD, LD == 8>(a.u32lo, col[q], xl);
+#pragma unroll
+        for (int st = 0; st < NST; ++st) {
+          const float p = __fmul_rn(vh[q], xh[st]);
+          float pe = __fmaf_rn(vh[q], xh[st], -p);
+          pe = __fmaf_rn(vh[q], xl[st], pe);
+          pe = __fmaf_rn(vl[q], xh[st], pe);
+          float t, err;
+          two_sum(ah[st], p, t, err);
+          ah[st] = t;
+          al[st] = __fadd_rn(al[st], __fadd_rn(err, pe));
+        }
+      }
+    }
+    float rh, rl;
+    reduce_scatter_ff<NP>(ah, al, lane, rh, rl);
+    const double hsum = (double)rh + (double)rl;
+    double ssum = 0.0;
+    const int64_t sb = a.s2ptr[k], se = a.s2ptr[k + 1];
+    const bool has_s2 = (j == 0) && (se > sb);
+    if (has_s2) {
+      float sh[NP], sl[NP];
+#pragma unroll
+      for (int st = 0; st < NP; ++st) sh[st] = sl[st] = 0.f;
+      for (int64_t e = sb + lane; e < se; e += 32) {
+        const float sv = __ldg(&a.s2val[e]);  // +-1: the products are exact
+        const int cj = __ldg(&a.s2col[e]);
+        float xh[NST], xl[NST];
+        load_row_ld<NST, LD, LD == 8>(a.u32, cj, xh);
+        load_row_ld<NST, LD, LD == 8>(a.u32lo, cj, xl);
+#pragma unroll
+        for (int st = 0; st < NST; ++st) {
+          float t, err;
+          two_sum(sh[st], sv * xh[st], t, err);
+          sh[st] = t;
+          sl[st] = __fadd_rn(sl[st], __fadd_rn(err, sv * xl[st]));
+        }
+      }
+      float qh, ql;
+      reduce_scatter_ff<NP>(sh, sl, lane, qh, ql);
+      ssum = (double)qh + (double)ql;
+    }
+    store_row<NST>(a, it, k, lane, hsum, ssum, has_s2);
+  }
+}
+
 template <int NST>
 void launch_sigma(const SigArgs& a, int precision, unsigned grid, cudaStream_t st, int n_sm, int variant) {
-  if (precision == QPGPU_FP32)
+  constexpr int P = Pow2<NST>::v;
+  if (precision == QPGPU_FF) {
+    const unsigned g = (unsigned)std::max<int64_t>(1, std::min<int64_t>((a.n_items * 32 + 127) / 128, 65535LL * 32));
+    k_sigma_ff<NST, P><<<g, 128, 0, st>>>(a);
+  } else if (precision == QPGPU_FP32)
     launch_sigma32<NST>(a, variant < 0 ? 0 : variant, st, n_sm);
   else
     k_sigma64<NST><<<grid, SBLK, 0, st>>>(a);
@@ -473,7 +580,7 @@ static int ensure_partials(qpgpu_ctx* c, SigmaItems* it, int nst) {
 
 int qp_sigma_launch(qpgpu_ctx* c, SigmaItems* it, double* v, double* s, const double* u, const float* u32, int nst,
                     int precision, cudaStream_t st, int row_lo, int row_hi, int row_first, int row_step,
-                    int u32_ld) {
+                    int u32_ld, const float* u32lo) {
   if (nst < 1 || nst > 8) return qpgpu_fail(c, QPGPU_ERR_ARG, "n_st must be in 1..8 per sigma block");
   if (c->direct) return qp_sigma_direct(c, v, s, u, nst, st, row_lo, row_hi, row_first, row_step);
   if (u32_ld <= 0) u32_ld = nst;
@@ -500,6 +607,10 @@ int qp_sigma_launch(qpgpu_ctx* c, SigmaItems* it, double* v, double* s, const do
   a.u = u;
   a.u32 = u32;
   a.u32_ld = u32_ld;
+  a.u32lo = u32lo;
+  a.val32lo = c->d_val32lo;
+  if (precision == QPGPU_FF && (!u32lo || !c->d_val32lo || u32_ld != qp_pad_states(nst)))
+    return qpgpu_fail(c, QPGPU_ERR_STATE, "float-float sigma needs split coefficients and elements");
   a.v = v;
   a.s = s;
   a.pv = it->pv;
@@ -530,6 +641,30 @@ void qp_to_bilinear(const double* u0, int64_t ld, const int* order, double* ut, 
 void qp_from_bilinear(const double* vt, int64_t ld, const int* order, double* v0, int nst, int64_t N,
                       cudaStream_t st) {
   k_from_bilinear<<<gsz(N * nst, 256), 256, 0, st>>>(vt, ld, order, v0, nst, N);
+}
+
+int qp_sigma_ff(qpgpu_ctx* c, SigmaItems* it, double* v, double* s, const double* u, int nst, cudaStream_t st,
+                int row_lo, int row_hi, int row_first, int row_step) {
+  if (nst < 1 || nst > 8) return qpgpu_fail(c, QPGPU_ERR_ARG, "n_st must be in 1..8 per sigma block");
+  if (c->direct) return qp_sigma_direct(c, v, s, u, nst, st, row_lo, row_hi, row_first, row_step);
+  const int64_t N = c->N;
+  if (!c->d_val32lo) {  // once per determinant set
+    QP_CUDA(c, dev_alloc(&c->d_val32lo, c->P));
+    k_lo_parts<<<gsz(c->P, 256), 256, 0, st>>>(c->d_val64, c->d_val32, c->d_val32lo, c->P);
+  }
+  const int ld = qp_pad_states(nst);
+  const size_t half = ((size_t)N * ld + 63) / 64 * 64;  // keeps lo 256-byte aligned
+  if (c->ffu_floats < 2 * half) {
+    dev_free(c->d_ffu);
+    c->d_ffu = nullptr;
+    c->ffu_floats = 0;
+    QP_CUDA(c, dev_alloc(&c->d_ffu, 2 * half));
+    c->ffu_floats = 2 * half;
+  }
+  float* hi = c->d_ffu;
+  float* lo = c->d_ffu + half;
+  k_split_rows<<<gsz(N * nst, 256), 256, 0, st>>>(u, hi, lo, N, nst, ld);
+  return qp_sigma_launch(c, it, v, s, u, hi, nst, QPGPU_FF, st, row_lo, row_hi, row_first, row_step, ld, lo);
 }
 
 void qp_to_float(const double* x, float* y, int64_t N, int nst, int ld, cudaStream_t st) {

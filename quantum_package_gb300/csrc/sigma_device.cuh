@@ -32,6 +32,35 @@ __device__ __forceinline__ double reduce_scatter64(double (&acc)[NSTP], int lane
   return x;
 }
 
+// Float-float (hi + lo) form of a double, built with integer and FP32
+// instructions only: hi keeps the top 24 bits of the significand
+// (truncated), lo the next 23 (the last 6 bits, below 2^-46 |x|, are
+// dropped), so hi + lo carries about 47 significant bits.  |x| below 2^-126
+// gives (0, 0) and below 2^-80 lo = 0, absolute errors far below anything a
+// Davidson vector resolves.  Finite |x| < 2^127 is assumed (normalised CI
+// vectors and their sigma).
+__device__ __forceinline__ void split_ff(double x, float& hi, float& lo) {
+  const unsigned long long b = (unsigned long long)__double_as_longlong(x);
+  const unsigned h32 = (unsigned)(b >> 32), l32 = (unsigned)b;
+  const unsigned sign = h32 & 0x80000000u;
+  const int e = (int)((h32 >> 20) & 0x7ffu);
+  const int fe = e - 896;  // float biased exponent of hi (e - 1023 + 127)
+  if (fe <= 0) {
+    hi = 0.f;
+    lo = 0.f;
+    return;
+  }
+  hi = __uint_as_float(sign | ((unsigned)fe << 23) | ((h32 & 0xfffffu) << 3) | (l32 >> 29));
+  const int se = e - 942;  // biased exponent of 2^(e - 1069)
+  if (se <= 0) {
+    lo = 0.f;
+    return;
+  }
+  const float r = __fsub_rn(__uint_as_float(0x4B000000u | ((l32 & 0x1fffffffu) >> 6)), 8388608.0f);
+  lo = __fmul_rn(r, __uint_as_float((unsigned)se << 23));
+  if (sign) lo = -lo;
+}
+
 // error-free sum of two floats (Knuth TwoSum)
 __device__ __forceinline__ void two_sum(float a, float b, float& s, float& e) {
   s = __fadd_rn(a, b);

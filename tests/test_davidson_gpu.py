@@ -65,3 +65,20 @@ def test_davidson_mixed_precision_within_1e6():
     assert np.abs(r32["energies"][:4] - r64["energies"][:4]).max() < 1e-6
     tr = r32["trace"]
     assert (tr["precision"] == FP32).any() and tr["precision"][-1] == FP64
+
+
+def test_davidson_float_float_restart_sigma():
+    # QPGPU_FF: FP32 sigma with the float-float sigma as the restart sigma;
+    # converged eigenvalues as accurate as the FP64 loop's
+    from quantum_package_gb300 import FF
+    from quantum_package_gb300.sigma import Wavefunction
+    p = G.make_problem(2, n_det=20_000, n_states=4)
+    wf = Wavefunction.from_problem(p)
+    u = _guess(p.n_det, 8, 3)
+    kw = dict(n_states=4, threshold=1e-12, s2_eig=False, max_iter=500)
+    r64 = wf.davidson_diag_hs2(u, **kw)
+    rff = wf.davidson_diag_hs2(u, precision=FF, **kw)
+    assert r64["converged"] and rff["converged"]
+    np.testing.assert_allclose(rff["energies"][:4], r64["energies"][:4], rtol=0, atol=1e-9)
+    tr = rff["trace"]
+    assert (tr["precision"] == FP32).any() and tr["precision"][-1] == FF

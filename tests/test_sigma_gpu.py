@@ -184,3 +184,21 @@ def test_u0_h_u0_matches_oracle():
     ref = np.einsum("ij,ij->i", u, v)
     assert e[1] == 0.0
     np.testing.assert_allclose(e[[0, 2]], ref[[0, 2]], rtol=REL64, atol=0)
+
+
+def test_sigma_float_float_vs_fp64():
+    # QPGPU_FF: float-float elements, coefficients and sums on the FP32 pipes
+    import torch
+    from quantum_package_gb300 import FF, FP64
+    p, o, wf = _problem(2, n_det=20_000, n_states=4)
+    for n_st in (3, 8):
+        u = G.random_coefficients(p.n_det, n_st, p.seed + n_st)
+        order = wf.bilinear_order()
+        ut = torch.from_numpy(np.ascontiguousarray(u[:, order].T)).cuda()
+        v64, s64, vff, sff = (torch.empty_like(ut) for _ in range(4))
+        wf.sigma_bilinear(v64, s64, ut, None, FP64)
+        wf.sigma_bilinear(vff, sff, ut, None, FF)
+        torch.cuda.synchronize()
+        a, b = v64.cpu().numpy(), vff.cpu().numpy()
+        _assert_sigma(b.T, a.T, REL64, f"FF n_st={n_st}")
+        _assert_sigma(sff.cpu().numpy().T, s64.cpu().numpy().T, REL64, f"FF S2 n_st={n_st}")
