@@ -220,10 +220,11 @@ def _guess(n, seed):
 
 
 def _time_to_e(res, e_ref, fp64):
-    """ms from the Davidson call until an FP64-sigma iteration has every state within E_TOL of e_ref."""
+    """ms from the Davidson call until an FP64 (or float-float) sigma iteration has every state within
+    E_TOL of e_ref; FP32-sigma iterations do not count."""
     tr = res["trace"]
     de = np.abs(tr["energies"] - e_ref[None, :]).max(axis=1)
-    ok = np.where((de < E_TOL) & (tr["precision"] == fp64))[0]
+    ok = np.where((de < E_TOL) & (tr["precision"] != 1))[0]  # FP64 or float-float iterations (not FP32)
     return (float(tr["elapsed_ms"][ok[0]]) if len(ok) else None), int(ok[0] + 1) if len(ok) else None
 
 
@@ -231,7 +232,7 @@ def davidson_block(prob, wf):
     """Time-to-E of the 4 lowest states: plain FP64 Davidson vs mixed precision vs
     mixed precision + learned preconditioner (trained on the first 1e4 and 2e5
     determinants of the same draw, as earlier CIPSI stages)."""
-    from quantum_package_gb300 import FP32, FP64
+    from quantum_package_gb300 import FF, FP32, FP64
     N = prob.n_det
     u = _guess(N, prob.seed)
     kw = dict(n_states=N_STATES, s2_eig=False, max_iter=400, davidson_sze_max=SZE_MAX)
@@ -257,6 +258,8 @@ def davidson_block(prob, wf):
 
     run("plain_fp64")
     run("mixed", precision=FP32)
+    # restart (defect-correction) sigma in float-float instead of FP64
+    run("mixed_ff_restart", precision=FF)
     # learned preconditioner: earlier stages of the same determinant draw
     t0 = time.perf_counter()
     wf.mlp_init(seed=3)
