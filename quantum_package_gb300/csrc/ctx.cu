@@ -235,7 +235,7 @@ int qpgpu_get_info(qpgpu_ctx* c, qpgpu_info* info) {
   const int64_t n = c->n_mo, N = c->N, P = c->P;
   int64_t b = 0;
   if (c->have_ints) b += 8 * (n * (n + 1) / 2) * (n * (n + 1) / 2 + 1) / 2 + 8 * (6 * n * n + 2 * n * n * n);
-  if (c->have_dets) b += N * (16 * c->nint + 4 * 8) + 8 * (int64_t)(c->Ua + c->Ub) * c->nint;
+  if (c->have_dets) b += N * (32 * c->nint + 4 * 8) + 8 * (int64_t)(c->Ua + c->Ub) * c->nint;
   if (c->have_pairs && !c->direct) b += P * 16 + c->P_s2 * 8 + N * 28;
   if (c->have_pairs && c->direct) b += N * 24;
   b += (int64_t)c->work_bytes;

@@ -353,7 +353,7 @@ void qp_free_dets(qpgpu_ctx* c) {
                  (void**)&c->d_cols, (void**)&c->d_order, (void**)&c->d_col_loc, (void**)&c->d_t_order,
                  (void**)&c->d_t_cols, (void**)&c->d_row_loc, (void**)&c->d_sa_ptr, (void**)&c->d_sa_idx,
                  (void**)&c->d_sb_ptr, (void**)&c->d_sb_idx, (void**)&c->d_cost_a, (void**)&c->d_cost_b,
-                 (void**)&c->d_detfeat};
+                 (void**)&c->d_detfeat, (void**)&c->d_alpha_pos, (void**)&c->d_beta_tpos};
   for (auto p : ps) {
     dev_free(*p);
     *p = nullptr;
@@ -361,6 +361,18 @@ void qp_free_dets(qpgpu_ctx* c) {
   c->have_dets = false;
   c->N = 0;
 }
+
+namespace {
+// out[i] = strings[id[p(i)]] (p = perm, or the identity), nint words each
+__global__ void k_gather_strings(const u64* strings, const int* id, const int* perm, u64* out, int64_t N, int nint) {
+  for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < N * nint; t += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t i = t / nint;
+    const int w = (int)(t % nint);
+    const int64_t p = perm ? perm[i] : i;
+    out[t] = strings[(int64_t)id[p] * nint + w];
+  }
+}
+}  // namespace
 
 // Requires c->d_dets and c->N set.
 int qp_build_index(qpgpu_ctx* c) {
@@ -409,6 +421,14 @@ int qp_build_index(qpgpu_ctx* c) {
     k_gather_int<<<grid_for(N), TPB, 0, st>>>(c->d_cols, c->d_t_order, c->d_t_cols, N);
     k_seg_starts<<<grid_for(N), TPB, 0, st>>>(trows.p, c->d_row_loc, N, Ua);
   }
+  // spin strings in scan order: the pair kernels read the strings of a
+  // column (row) as one contiguous span instead of index -> string gathers
+  QP_CUDA(c, dev_alloc(&c->d_alpha_pos, (size_t)N * c->nint));
+  QP_CUDA(c, dev_alloc(&c->d_beta_tpos, (size_t)N * c->nint));
+  k_gather_strings<<<grid_for(N * c->nint), TPB, 0, st>>>(c->d_alpha, c->d_rows, nullptr, c->d_alpha_pos, N,
+                                                          c->nint);
+  k_gather_strings<<<grid_for(N * c->nint), TPB, 0, st>>>(c->d_beta, c->d_cols, c->d_t_order, c->d_beta_tpos, N,
+                                                          c->nint);
   qp_mark(c, "bilinear index");
   // singles among unique strings, and the per-string costs of the two
   // alpha-beta scan strategies

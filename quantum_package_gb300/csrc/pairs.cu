@@ -53,6 +53,8 @@ struct BuildArgs {
   const int* t_order;
   const int* t_cols;
   const int* row_loc;
+  const u64* alpha_pos;  // alpha string at each bilinear position
+  const u64* beta_tpos;  // beta string at each alpha-major position
   const int* sa_ptr;
   const int* sa_idx;
   const int* sb_ptr;
@@ -130,11 +132,7 @@ __global__ void __launch_bounds__(BLK) k_class_a(BuildArgs a) {
   for (int t0 = U0; t0 < U1; t0 += TILE) {
     const int tn = min(TILE, U1 - t0);
     __syncthreads();
-    for (int i = threadIdx.x; i < tn; i += BLK) {
-      const int ai = a.rows[t0 + i];
-#pragma unroll
-      for (int w = 0; w < NINT; ++w) tile[i * NINT + w] = a.alpha[(int64_t)ai * NINT + w];
-    }
+    for (int i = threadIdx.x; i < tn * NINT; i += BLK) tile[i] = a.alpha_pos[(int64_t)t0 * NINT + i];
     __syncthreads();
     if (act) {
       const int lo = max(cs, t0), hi = min(ce, t0 + tn);
@@ -206,11 +204,7 @@ __global__ void __launch_bounds__(BLK) k_class_b(BuildArgs a) {
   for (int t0 = V0; t0 < V1; t0 += TILE) {
     const int tn = min(TILE, V1 - t0);
     __syncthreads();
-    for (int i = threadIdx.x; i < tn; i += BLK) {
-      const int bi = a.t_cols[t0 + i];
-#pragma unroll
-      for (int w = 0; w < NINT; ++w) tile[i * NINT + w] = a.beta[(int64_t)bi * NINT + w];
-    }
+    for (int i = threadIdx.x; i < tn * NINT; i += BLK) tile[i] = a.beta_tpos[(int64_t)t0 * NINT + i];
     __syncthreads();
     if (act) {
       const int lo = max(rs, t0), hi = min(re, t0 + tn);
@@ -300,11 +294,10 @@ __global__ void __launch_bounds__(BLK) k_class_c(BuildArgs a) {
           bool hit = false;
           u64 ca[NINT];
           if (pos < end) {
-            const int ap = a.rows[pos];
             int d = 0;
 #pragma unroll
             for (int w = 0; w < NINT; ++w) {
-              ca[w] = a.alpha[(int64_t)ap * NINT + w];
+              ca[w] = a.alpha_pos[(int64_t)pos * NINT + w];
               d += popc64(my[w] ^ ca[w]);
             }
             hit = (d == 2);
@@ -367,11 +360,10 @@ __global__ void __launch_bounds__(BLK) k_class_c(BuildArgs a) {
           bool hit = false;
           u64 cb[NINT];
           if (q < end) {
-            const int bp = a.t_cols[q];
             int d = 0;
 #pragma unroll
             for (int w = 0; w < NINT; ++w) {
-              cb[w] = a.beta[(int64_t)bp * NINT + w];
+              cb[w] = a.beta_tpos[(int64_t)q * NINT + w];
               d += popc64(my[NINT + w] ^ cb[w]);
             }
             hit = (d == 2);
@@ -491,6 +483,8 @@ BuildArgs index_args(const qpgpu_ctx* c) {
   a.t_order = c->d_t_order;
   a.t_cols = c->d_t_cols;
   a.row_loc = c->d_row_loc;
+  a.alpha_pos = c->d_alpha_pos;
+  a.beta_tpos = c->d_beta_tpos;
   a.sa_ptr = c->d_sa_ptr;
   a.sa_idx = c->d_sa_idx;
   a.sb_ptr = c->d_sb_ptr;

@@ -382,6 +382,8 @@ struct qpgpu_ctx {
   int* d_t_order = nullptr;    // alpha-major position -> bilinear position
   int* d_t_cols = nullptr;     // alpha-major position -> beta id
   int* d_row_loc = nullptr;    // (U_a+1) first alpha-major position of each alpha row
+  u64* d_alpha_pos = nullptr;  // (N, nint) alpha string at each bilinear position (coalesced scans)
+  u64* d_beta_tpos = nullptr;  // (N, nint) beta string at each alpha-major position
   int* d_sa_ptr = nullptr;     // singles adjacency of unique alpha strings (CSR)
   int* d_sa_idx = nullptr;
   int* d_sb_ptr = nullptr;
