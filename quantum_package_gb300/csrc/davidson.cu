@@ -1104,15 +1104,15 @@ extern "C" int qpgpu_davidson_hs2(qpgpu_ctx* c, double* u_in, int64_t dim_in, do
         if (r > 1e8 || !std::isfinite(r)) failed = true;  // 'Davidson failed' (:404-409)
       }
       // fallback: a state whose residual (the reference's measure, from the
-      // diagonal correction) failed to fall by at least 5% in two consecutive
-      // learned steps goes back to the diagonal step for the rest of the run.
+      // diagonal correction) fails to fall by at least 5% after a learned step
+      // goes back to the diagonal step for the rest of the run.
       // The first iteration of a restart cycle is not judged: its residual
       // comes from the re-contracted basis (and, in mixed precision, from the
       // cycle's first FP64 sigma), not from the preceding step.
       for (int k = 0; k < nst; ++k) {
         if (mlp_on[k] && iter > 1) {
           strikes[k] = (res[k] > 0.95 * prev_res[k]) ? strikes[k] + 1 : 0;
-          if (strikes[k] >= 2) {
+          if (strikes[k] >= 1) {
             mlp_on[k] = false;
             ++n_fallback;
           }
