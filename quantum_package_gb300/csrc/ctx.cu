@@ -214,6 +214,7 @@ int qpgpu_destroy(qpgpu_ctx* c) {
     dev_free(c->d_work);
     dev_free(c->d_stage);
     dev_free(c->d_ffu);
+    dev_free(c->d_direct_ut);
     cudaStreamDestroy(c->stream);
   }
   delete c;

@@ -77,6 +77,7 @@ struct BuildArgs {
   int* err;  // set when a fill pass would write past its row's segment
   // direct sigma (MODE_SIGMA): v, s = H u, S^2 u for the selected rows, u (N, nst)
   const double* u;
+  const double* uT;  // u in alpha-major order: same-alpha partners are contiguous there
   double* v;
   double* s;
   const double* hdiag;
@@ -91,7 +92,13 @@ __device__ __forceinline__ bool dsel(const BuildArgs& a, int64_t k) {
   return k >= a.row_lo && k < a.row_hi && ((k - a.row_first) % a.row_step) == 0;
 }
 
-// acc[st] += h * u[j][st]
+// acc[st] += h * u[j][st] (j bilinear position; dacc_t: alpha-major position)
+__device__ __forceinline__ void dacc_t(const BuildArgs& a, double h, int64_t q, double (&acc)[8]) {
+  const double* uj = a.uT + q * a.nst;
+#pragma unroll
+  for (int st = 0; st < 8; ++st)
+    if (st < a.nst) acc[st] = fma(h, __ldg(uj + st), acc[st]);
+}
 __device__ __forceinline__ void dacc(const BuildArgs& a, double h, int64_t j, double (&acc)[8]) {
   const double* uj = a.u + j * a.nst;
 #pragma unroll
@@ -224,7 +231,7 @@ __global__ void __launch_bounds__(BLK) k_class_b(BuildArgs a) {
             double v = (d == 2) ? h_mono_spin<NINT>(a.t, my, J, 2, nullptr, nullptr)
                                 : h_double_spin<NINT>(a.t, my + NINT, c, nullptr, nullptr);
             if (SIG) {
-              dacc(a, v, a.t_order[pos], acc);
+              dacc_t(a, v, pos, acc);
             } else if (cnt < a.cntB[k]) {
               a.colidx[out + cnt] = a.t_order[pos];
               a.val64[out + cnt] = v;
@@ -380,8 +387,8 @@ __global__ void __launch_bounds__(BLK) k_class_c(BuildArgs a) {
             }
             double s2;
             const double v = h_double_ab<NINT>(a.t, my, J, &s2, nullptr, nullptr);
-            dacc(a, v, a.t_order[q], acc);
-            if (flip) dacc(a, s2, a.t_order[q], sacc);
+            dacc_t(a, v, q, acc);
+            if (flip) dacc_t(a, s2, q, sacc);
           }
           if (FILL && hit) {
             u64 J[2 * NINT];
@@ -601,11 +608,17 @@ int build_pairs_t(qpgpu_ctx* c) {
   return 0;
 }
 
+__global__ void k_alpha_major(const double* u, const int* t_order, double* uT, int64_t N, int nst) {
+  for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < N * nst; t += (int64_t)gridDim.x * blockDim.x)
+    uT[t] = u[(int64_t)t_order[t / nst] * nst + t % nst];
+}
+
 template <int NINT>
-void sigma_direct_t(qpgpu_ctx* c, double* v, double* s, const double* u, int nst, cudaStream_t st, int row_lo,
-                    int row_hi, int row_first, int row_step) {
+void sigma_direct_t(qpgpu_ctx* c, double* v, double* s, const double* u, const double* uT, int nst,
+                    cudaStream_t st, int row_lo, int row_hi, int row_first, int row_step) {
   BuildArgs a = index_args(c);
   a.u = u;
+  a.uT = uT;
   a.v = v;
   a.s = s;
   a.hdiag = c->d_hdiag;
@@ -630,10 +643,19 @@ int qp_sigma_direct(qpgpu_ctx* c, double* v, double* s, const double* u, int nst
                     int row_hi, int row_first, int row_step) {
   if (nst < 1 || nst > 8) return qpgpu_fail(c, QPGPU_ERR_ARG, "n_st must be in 1..8 per sigma block");
   if (row_step < 1) return qpgpu_fail(c, QPGPU_ERR_ARG, "row step must be >= 1");
+  const size_t need = (size_t)c->N * nst;
+  if (c->direct_ut_n < need) {
+    dev_free(c->d_direct_ut);
+    c->d_direct_ut = nullptr;
+    c->direct_ut_n = 0;
+    QP_CUDA(c, dev_alloc(&c->d_direct_ut, need));
+    c->direct_ut_n = need;
+  }
+  k_alpha_major<<<nblocks((int64_t)need, 256), 256, 0, st>>>(u, c->d_t_order, c->d_direct_ut, c->N, nst);
   if (c->nint == 1)
-    sigma_direct_t<1>(c, v, s, u, nst, st, row_lo, row_hi, row_first, row_step);
+    sigma_direct_t<1>(c, v, s, u, c->d_direct_ut, nst, st, row_lo, row_hi, row_first, row_step);
   else
-    sigma_direct_t<2>(c, v, s, u, nst, st, row_lo, row_hi, row_first, row_step);
+    sigma_direct_t<2>(c, v, s, u, c->d_direct_ut, nst, st, row_lo, row_hi, row_first, row_step);
   QP_CUDA(c, cudaGetLastError());
   return 0;
 }

@@ -397,6 +397,8 @@ struct qpgpu_ctx {
   bool have_pairs = false;
   int sigma_mode = QPGPU_SIGMA_AUTO;  // qpgpu_set_sigma_mode
   bool direct = false;                // pairs not stored: sigma enumerates them (pairs.cu)
+  double* d_direct_ut = nullptr;      // direct sigma: u in alpha-major order
+  size_t direct_ut_n = 0;
   int64_t P = 0;
   int64_t* d_rowptr = nullptr;  // N+1
   int* d_colidx = nullptr;      // P
