@@ -241,74 +241,72 @@ __device__ __forceinline__ double* barr(const BProb& P, int sel) {
 
 // partial Gram G[i][j] = sum_r A_i[r] B_j[r]: A = blocks a0..a0+nbA-1 of array
 // asel, B = block bb of array bsel; rows [c*BROWS, ...) of CTA c; one partial
-// per (problem, CTA).  Register tile of CI columns x nsd, fixed-order sums.
-constexpr int BGTR = 32;
-template <int CI>
-__global__ void __launch_bounds__(BBLK) k_bgram(const BProb* __restrict__ probs, int nsd, int asel, int a0, int nbA,
-                                                int bsel, int bb, double* partial, int pstride,
+// per (problem, CTA).  As the single-problem k_gram: a lane owns one row at a
+// time and CI = 32 / NSD columns of A for all NSD columns of B (every FP64 FMA
+// useful), warps hold column groups (or split the rows when there are fewer
+// groups), gridDim.z passes cover the rest, and the sums are combined in a
+// fixed order (reduce-scatter over lanes, shared memory over warps).
+template <int NSD>
+__global__ void __launch_bounds__(BBLK) k_bgram(const BProb* __restrict__ probs, int asel, int a0, int nbA, int bsel,
+                                                int bb, double* partial, int pstride,
                                                 const int* skip /* per problem, stride sstride */, int sstride,
                                                 int ncta_max) {
-  extern __shared__ double sm[];
+  constexpr int CI = 32 / NSD;
+  constexpr int NW = BBLK / 32;
+  __shared__ double red[NW][32];
   const BProb& P = probs[blockIdx.y];
   const int c = blockIdx.x;
   if (!P.active || c >= P.ncta) return;
-  const int m = nbA * nsd, np = m * nsd;
+  const int m = nbA * NSD;
+  const int ncg = (m + CI - 1) / CI;
+  const int cg0 = blockIdx.z * NW;
+  if (cg0 >= ncg) return;
   double* out = partial + ((int64_t)blockIdx.y * ncta_max + c) * pstride;
   if (skip && skip[(int64_t)blockIdx.y * sstride]) {
-    for (int p = threadIdx.x; p < np; p += BBLK) out[p] = 0.0;
+    for (int p = cg0 * CI * NSD + threadIdx.x; p < min(m, (cg0 + NW) * CI) * NSD; p += BBLK) out[p] = 0.0;
     return;
   }
   const int64_t N = P.N;
-  const double* A = barr(P, asel) + (int64_t)a0 * N * nsd;
-  const double* B = barr(P, bsel) + (int64_t)bb * N * nsd;
-  double* As = sm;
-  double* Bs = sm + BGTR * m;
+  const double* A = barr(P, asel) + (int64_t)a0 * N * NSD;
+  const double* B = barr(P, bsel) + (int64_t)bb * N * NSD;
+  const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int ncg_here = min(NW, ncg - cg0);
+  const int rg = NW / ncg_here;
+  const int cgl = w % ncg_here, rgi = w / ncg_here;
+  const bool act = rgi < rg;
+  const int cg = cg0 + cgl;
+  const int nq = min(CI, m - cg * CI);
+  const double* ap[CI];
+#pragma unroll
+  for (int q = 0; q < CI; ++q) {
+    const int i = min(cg * CI + q, m - 1);
+    ap[q] = A + (int64_t)(i / NSD) * N * NSD + (i % NSD);
+  }
+  double acc[32];
+#pragma unroll
+  for (int k = 0; k < 32; ++k) acc[k] = 0.0;
   const int64_t r0 = (int64_t)c * BROWS, r1 = min(r0 + BROWS, N);
-  const int ncol = m / CI;
-  const int groups = min(BBLK / ncol, BGTR);
-  const int ci = threadIdx.x % ncol, g = threadIdx.x / ncol;
-  const bool act = g < groups;
-  double acc[CI][BMAXS];
+  if (act) {
+    for (int64_t r = r0 + (int64_t)rgi * 32 + lane; r < r1; r += (int64_t)rg * 32) {
+      double a[CI], b[NSD];
 #pragma unroll
-  for (int a = 0; a < CI; ++a)
+      for (int q = 0; q < CI; ++q) a[q] = (q < nq) ? ap[q][r * NSD] : 0.0;
+      load_row<NSD>(B, r, b);
 #pragma unroll
-    for (int j = 0; j < BMAXS; ++j) acc[a][j] = 0.0;
-  for (int64_t t0 = r0; t0 < r1; t0 += BGTR) {
-    const int tr = (int)min((int64_t)BGTR, r1 - t0);
-    __syncthreads();
-    for (int idx = threadIdx.x; idx < nbA * tr * nsd; idx += BBLK) {
-      const int b = idx / (tr * nsd), rem = idx % (tr * nsd), r = rem / nsd, cc = rem % nsd;
-      As[r * m + b * nsd + cc] = A[(int64_t)b * N * nsd + (t0 + r) * nsd + cc];
-    }
-    for (int idx = threadIdx.x; idx < tr * nsd; idx += BBLK) Bs[idx] = B[t0 * nsd + idx];
-    __syncthreads();
-    if (act) {
-      for (int r = g; r < tr; r += groups) {
-        double a[CI];
+      for (int q = 0; q < CI; ++q)
+        if (q < nq)
 #pragma unroll
-        for (int q = 0; q < CI; ++q) a[q] = As[r * m + ci * CI + q];
-#pragma unroll
-        for (int j = 0; j < BMAXS; ++j) {
-          if (j < nsd) {
-            const double bv = Bs[r * nsd + j];
-#pragma unroll
-            for (int q = 0; q < CI; ++q) acc[q][j] = fma(a[q], bv, acc[q][j]);
-          }
-        }
-      }
+          for (int j = 0; j < NSD; ++j) acc[q * NSD + j] = fma(a[q], b[j], acc[q * NSD + j]);
     }
   }
+  const double v = reduce_scatter64<32>(acc, lane);  // lane L: entry (L / NSD, L % NSD)
+  if (act) red[w][lane] = v;
   __syncthreads();
-  double* red = sm;
-  if (act)
-#pragma unroll
-    for (int q = 0; q < CI; ++q)
-      for (int j = 0; j < nsd; ++j) red[((size_t)g * m + ci * CI + q) * nsd + j] = acc[q][j];
-  __syncthreads();
-  for (int p = threadIdx.x; p < np; p += BBLK) {
-    double s = 0.0;
-    for (int q = 0; q < groups; ++q) s += red[(size_t)q * np + p];
-    out[p] = s;
+  if (w < ncg_here) {
+    double t = 0.0;
+    for (int g = 0; g < rg; ++g) t += red[g * ncg_here + w][lane];
+    const int q = lane / NSD, j = lane % NSD, i = cg * CI + q;
+    if (q < CI && i < m) out[(int64_t)i * NSD + j] = t;
   }
 }
 
@@ -334,10 +332,13 @@ struct BLin {
   int asel[3], osel[3], oblk[3];
   int n;
 };
+// NSD = nsd exactly (no predicated columns: on GB300 every FP64 FMA slot
+// counts); a thread reads its whole row of each block (16-byte loads for even
+// NSD) before it writes, so out may alias the last block of A.
+template <int NSD>
 __global__ void __launch_bounds__(BBLK) k_blincomb(const BProb* __restrict__ probs, BLin L, int a0, int m_uniform,
-                                                   const int* m_per /* nullable */, int nsd, const double* C,
-                                                   int cstride, int sub, const int* skip, int sstride,
-                                                   int include_inactive) {
+                                                   const int* m_per /* nullable */, const double* C, int cstride,
+                                                   int sub, const int* skip, int sstride, int include_inactive) {
   const BProb& P = probs[blockIdx.y];
   if (!P.active && !include_inactive) return;
   if (skip && skip[(int64_t)blockIdx.y * sstride]) return;
@@ -345,29 +346,49 @@ __global__ void __launch_bounds__(BBLK) k_blincomb(const BProb* __restrict__ pro
   if (m <= 0) return;
   __shared__ double Cs[BMAXM * BMAXS];
   const double* Cp = C + (int64_t)blockIdx.y * cstride;
-  for (int i = threadIdx.x; i < m * nsd; i += BBLK) Cs[i] = Cp[i];
+  for (int i = threadIdx.x; i < m * NSD; i += BBLK) Cs[i] = Cp[i];
   __syncthreads();
   const int64_t N = P.N;
-  const int nb = m / nsd;
+  const int nb = m / NSD;
   for (int64_t r = blockIdx.x * (int64_t)BBLK + threadIdx.x; r < N; r += (int64_t)gridDim.x * BBLK) {
     for (int t = 0; t < L.n; ++t) {
-      const double* A = barr(P, L.asel[t]) + (int64_t)a0 * N * nsd;
-      double acc[BMAXS];
+      const double* A = barr(P, L.asel[t]) + (int64_t)a0 * N * NSD;
+      double acc[NSD];
 #pragma unroll
-      for (int j = 0; j < BMAXS; ++j) acc[j] = 0.0;
+      for (int j = 0; j < NSD; ++j) acc[j] = 0.0;
       for (int b = 0; b < nb; ++b) {
-        const double* a = A + (int64_t)b * N * nsd + r * nsd;
-        for (int cc = 0; cc < nsd; ++cc) {
-          const double x = a[cc];
-          const double* crow = &Cs[(b * nsd + cc) * nsd];
+        double x[NSD];
+        load_row<NSD>(A + (int64_t)b * N * NSD, r, x);
+        const double* cb = &Cs[b * NSD * NSD];
 #pragma unroll
-          for (int j = 0; j < BMAXS; ++j)
-            if (j < nsd) acc[j] = fma(x, crow[j], acc[j]);
-        }
+        for (int cc = 0; cc < NSD; ++cc)
+#pragma unroll
+          for (int j = 0; j < NSD; ++j) acc[j] = fma(x[cc], cb[cc * NSD + j], acc[j]);
       }
-      double* o = barr(P, L.osel[t]) + (int64_t)L.oblk[t] * N * nsd + r * nsd;
-      for (int j = 0; j < nsd; ++j) o[j] = sub ? o[j] - acc[j] : acc[j];
+      double* o = barr(P, L.osel[t]) + (int64_t)L.oblk[t] * N * NSD + r * NSD;
+#pragma unroll
+      for (int j = 0; j < NSD; ++j) o[j] = sub ? o[j] - acc[j] : acc[j];
     }
+  }
+}
+
+void launch_blincomb(dim3 grid, cudaStream_t st, int nsd, const BProb* probs, BLin L, int a0, int m,
+                     const int* mper, const double* C, int cstride, int sub, const int* skip, int sstride,
+                     int include_inactive) {
+  switch (nsd) {
+#define QP_BLC(NS)                                                                                                \
+  case NS:                                                                                                        \
+    k_blincomb<NS><<<grid, BBLK, 0, st>>>(probs, L, a0, m, mper, C, cstride, sub, skip, sstride, include_inactive); \
+    break;
+    QP_BLC(1)
+    QP_BLC(2)
+    QP_BLC(3)
+    QP_BLC(4)
+    QP_BLC(5)
+    QP_BLC(6)
+    QP_BLC(7)
+    QP_BLC(8)
+#undef QP_BLC
   }
 }
 
@@ -553,17 +574,25 @@ struct BDav {
 void bgram(BDav& D, int asel, int a0, int nbA, int bsel, int bb, int out_off, const int* skip) {
   qpgpu_batch* B = D.B;
   const int m = nbA * D.nsd;
-  const int ci = (m % 4 == 0) ? 4 : (m % 2 == 0) ? 2 : 1;
-  const int groups = std::min(BBLK / (m / ci), BGTR);
-  const size_t shm = std::max((size_t)BGTR * (m + D.nsd), (size_t)groups * m * D.nsd) * sizeof(double);
-  const dim3 grid(D.ncta_max, B->np);
+  const int ci = 32 / D.nsd;
+  const int ncg = (m + ci - 1) / ci;
+  const dim3 grid(D.ncta_max, B->np, (ncg + BBLK / 32 - 1) / (BBLK / 32));
   const int ss = SMALL * 2;
-  if (ci == 4)
-    k_bgram<4><<<grid, BBLK, shm, B->st>>>(B->d, D.nsd, asel, a0, nbA, bsel, bb, D.part, 512, skip, ss, D.ncta_max);
-  else if (ci == 2)
-    k_bgram<2><<<grid, BBLK, shm, B->st>>>(B->d, D.nsd, asel, a0, nbA, bsel, bb, D.part, 512, skip, ss, D.ncta_max);
-  else
-    k_bgram<1><<<grid, BBLK, shm, B->st>>>(B->d, D.nsd, asel, a0, nbA, bsel, bb, D.part, 512, skip, ss, D.ncta_max);
+  switch (D.nsd) {
+#define QP_BG(NS)                                                                                          \
+  case NS:                                                                                                 \
+    k_bgram<NS><<<grid, BBLK, 0, B->st>>>(B->d, asel, a0, nbA, bsel, bb, D.part, 512, skip, ss, D.ncta_max); \
+    break;
+    QP_BG(1)
+    QP_BG(2)
+    QP_BG(3)
+    QP_BG(4)
+    QP_BG(5)
+    QP_BG(6)
+    QP_BG(7)
+    QP_BG(8)
+#undef QP_BG
+  }
   k_breduce<<<dim3(gsz((int64_t)m * D.nsd * 32), B->np), BBLK, 0, B->st>>>(B->d, D.part, 512, D.ncta_max, m * D.nsd,
                                                                            D.small + out_off, SMALL);
 }
@@ -571,8 +600,8 @@ void bgram(BDav& D, int asel, int a0, int nbA, int bsel, int bb, int out_off, co
 void blin(BDav& D, BLin L, int a0, int m, const int* mper, int coff, int sub, const int* skip, int include_inactive,
           int64_t maxN) {
   qpgpu_batch* B = D.B;
-  k_blincomb<<<dim3(gsz(maxN), B->np), BBLK, 0, B->st>>>(B->d, L, a0, m, mper, D.nsd, D.small + coff, SMALL, sub, skip,
-                                                          SMALL * 2, include_inactive);
+  launch_blincomb(dim3(gsz(maxN), B->np), B->st, D.nsd, B->d, L, a0, m, mper, D.small + coff, SMALL, sub, skip,
+                  SMALL * 2, include_inactive);
 }
 
 // device part of an iteration before the small eigenproblems: orthonormalise
@@ -658,9 +687,6 @@ int qpgpu_batch_create(qpgpu_ctx* const* ctxs, int n, qpgpu_batch** out) {
     return QPGPU_ERR_CUDA;
   }
   // the fixed-order group reduction of k_bgram uses up to 64 KB of shared memory
-  cudaFuncSetAttribute(k_bgram<4>, cudaFuncAttributeMaxDynamicSharedMemorySize, 96 * 1024);
-  cudaFuncSetAttribute(k_bgram<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, 96 * 1024);
-  cudaFuncSetAttribute(k_bgram<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, 96 * 1024);
   B->h.resize(n);
   int64_t base = 0;
   for (int i = 0; i < n; ++i) {
@@ -935,8 +961,7 @@ int qpgpu_batch_davidson(qpgpu_batch* B, double* const* u_in, const int64_t* dim
     QB_CUDA(B, cudaMemcpyAsync(D.mper, mper.data(), np * sizeof(int), cudaMemcpyHostToDevice, st));
     QB_CUDA(B, cudaMemcpyAsync(D.copyf, copyf.data(), np * sizeof(int), cudaMemcpyHostToDevice, st));
     BLin L{{AU, 0, 0}, {AR, 0, 0}, {0, 0, 0}, 1};
-    k_blincomb<<<dim3(gsz(maxN), np), BBLK, 0, st>>>(B->d, L, 0, shift2, D.mper, nsd, D.small + O_Y, SMALL, 0,
-                                                     nullptr, 0, 1);
+    launch_blincomb(dim3(gsz(maxN), np), st, nsd, B->d, L, 0, shift2, D.mper, D.small + O_Y, SMALL, 0, nullptr, 0, 1);
     k_bcopy_block<<<dim3(gsz(maxN * nsd), np), BBLK, 0, st>>>(B->d, nsd, D.copyf);
     QB_CUDA(B, cudaGetLastError());
     for (int p = 0; p < np; ++p) {
