@@ -16,6 +16,7 @@ def test_create_rejects_bad_shapes_without_gpu_work():
     L = _lib.load()
     h = ctypes.c_void_p()
     assert L.qpgpu_create(300, 2, 2, 5, ctypes.byref(h)) == -1      # n_mo too large
+    assert L.qpgpu_create(129, 4, 4, 3, ctypes.byref(h)) == -1      # N_int = 3 (n_mo <= 128 supported)
     assert L.qpgpu_create(80, 14, 14, 1, ctypes.byref(h)) == -1     # wrong n_int
     assert L.qpgpu_create(80, 10, 12, 2, ctypes.byref(h)) == -1     # n_alpha < n_beta
     assert L.qpgpu_destroy(None) == -1

@@ -145,8 +145,9 @@ def test_edge_cases():
     o = Oracle(8, 3, 1, ints8.h, ints8.eri, d)
     u = np.random.default_rng(0).normal(size=(1, len(d)))
     _assert_sigma(wf.H_S2_u_0_nstates_openmp(u)[0], o.h_s2_u0(u)[0], REL64, "single column")
-    # n_mo = 64 (one full word) and 65 (second word with a single bit)
-    for n in (64, 65):
+    # n_mo = 64 (one full word), 65 (second word with a single bit) and 128
+    # (the largest supported space: both words full)
+    for n in (64, 65, 128):
         p = G.make_problem(1, n_det=3000, n_mo=n, n_alpha=6, n_beta=5)
         wf = _wf(p.n_mo, 6, 5, p.ints, p.dets)
         o = Oracle.from_problem(p)
@@ -171,6 +172,8 @@ def test_invalid_inputs_raise():
     bad[0, 1, 0] = np.uint64((1 << 12) | 3)  # orbital 13 > n_mo
     with pytest.raises(QPGPUError):
         wf.set_dets(bad)
+    with pytest.raises(QPGPUError):  # empty determinant set
+        wf.set_dets(np.zeros((0, 2, 1), np.uint64))
 
 
 def test_u0_h_u0_matches_oracle():
