@@ -149,24 +149,21 @@ __global__ void __launch_bounds__(BLK) k_class_a(BuildArgs a) {
 #pragma unroll
         for (int w = 0; w < NINT; ++w) d += popc64(my[w] ^ c[w]);
         if (d == 2 || d == 4) {
-          if (FILL || SIG) {
+          if (SIG) {
             u64 J[2 * NINT];
 #pragma unroll
             for (int w = 0; w < NINT; ++w) {
               J[w] = c[w];
               J[NINT + w] = my[NINT + w];
             }
-            double v = (d == 2) ? h_mono_spin<NINT>(a.t, my, J, 1, nullptr, nullptr)
-                                : h_double_spin<NINT>(a.t, my, c, nullptr, nullptr);
-            if (SIG) {
-              dacc(a, v, pos, acc);
-            } else if (cnt < a.cntA[k]) {
+            const double v = (d == 2) ? h_mono_spin<NINT>(a.t, my, J, 1, nullptr, nullptr)
+                                      : h_double_spin<NINT>(a.t, my, c, nullptr, nullptr);
+            dacc(a, v, pos, acc);
+          } else if (FILL) {  // elements: k_pair_values
+            if (cnt < a.cntA[k])
               a.colidx[out + cnt] = pos;
-              a.val64[out + cnt] = v;
-              a.val32[out + cnt] = (float)v;
-            } else {
+            else
               atomicOr(a.err, 1);
-            }
           }
           ++cnt;
         }
@@ -221,24 +218,21 @@ __global__ void __launch_bounds__(BLK) k_class_b(BuildArgs a) {
 #pragma unroll
         for (int w = 0; w < NINT; ++w) d += popc64(my[NINT + w] ^ c[w]);
         if (d == 2 || d == 4) {
-          if (FILL || SIG) {
+          if (SIG) {
             u64 J[2 * NINT];
 #pragma unroll
             for (int w = 0; w < NINT; ++w) {
               J[w] = my[w];
               J[NINT + w] = c[w];
             }
-            double v = (d == 2) ? h_mono_spin<NINT>(a.t, my, J, 2, nullptr, nullptr)
-                                : h_double_spin<NINT>(a.t, my + NINT, c, nullptr, nullptr);
-            if (SIG) {
-              dacc_t(a, v, pos, acc);
-            } else if (cnt < a.cntB[k]) {
+            const double v = (d == 2) ? h_mono_spin<NINT>(a.t, my, J, 2, nullptr, nullptr)
+                                      : h_double_spin<NINT>(a.t, my + NINT, c, nullptr, nullptr);
+            dacc_t(a, v, pos, acc);
+          } else if (FILL) {  // elements: k_pair_values
+            if (cnt < a.cntB[k])
               a.colidx[out + cnt] = a.t_order[pos];
-              a.val64[out + cnt] = v;
-              a.val32[out + cnt] = (float)v;
-            } else {
+            else
               atomicOr(a.err, 2);
-            }
           }
           ++cnt;
         }
@@ -324,24 +318,21 @@ __global__ void __launch_bounds__(BLK) k_class_c(BuildArgs a) {
             dacc(a, v, pos, acc);
             if (flip) dacc(a, s2, pos, sacc);
           }
-          if (FILL && hit) {
-            u64 J[2 * NINT];
-#pragma unroll
-            for (int w = 0; w < NINT; ++w) {
-              J[w] = ca[w];
-              J[NINT + w] = cb[w];
-            }
-            double s2;
-            const double v = h_double_ab<NINT>(a.t, my, J, &s2, nullptr, nullptr);
+          if (FILL && hit) {  // elements: k_pair_values; S^2 values of spin flips here
             const int64_t o = out + cnt + __popc(bal & lt);
-            if (o < a.rowptr[k + 1]) {
+            if (o < a.rowptr[k + 1])
               a.colidx[o] = pos;
-              a.val64[o] = v;
-              a.val32[o] = (float)v;
-            } else {
+            else
               atomicOr(a.err, 4);
-            }
             if (flip) {
+              u64 J[2 * NINT];
+#pragma unroll
+              for (int w = 0; w < NINT; ++w) {
+                J[w] = ca[w];
+                J[NINT + w] = cb[w];
+              }
+              double s2;
+              h_double_ab<NINT>(a.t, my, J, &s2, nullptr, nullptr);
               const int64_t so = sout + scnt + __popc(sbal & lt);
               if (so < a.s2ptr[k + 1]) {
                 a.s2col[so] = pos;
@@ -390,25 +381,22 @@ __global__ void __launch_bounds__(BLK) k_class_c(BuildArgs a) {
             dacc_t(a, v, q, acc);
             if (flip) dacc_t(a, s2, q, sacc);
           }
-          if (FILL && hit) {
-            u64 J[2 * NINT];
-#pragma unroll
-            for (int w = 0; w < NINT; ++w) {
-              J[w] = ca[w];
-              J[NINT + w] = cb[w];
-            }
-            double s2;
-            const double v = h_double_ab<NINT>(a.t, my, J, &s2, nullptr, nullptr);
+          if (FILL && hit) {  // elements: k_pair_values; S^2 values of spin flips here
             const int64_t o = out + cnt + __popc(bal & lt);
             const int jpos = a.t_order[q];
-            if (o < a.rowptr[k + 1]) {
+            if (o < a.rowptr[k + 1])
               a.colidx[o] = jpos;
-              a.val64[o] = v;
-              a.val32[o] = (float)v;
-            } else {
+            else
               atomicOr(a.err, 4);
-            }
             if (flip) {
+              u64 J[2 * NINT];
+#pragma unroll
+              for (int w = 0; w < NINT; ++w) {
+                J[w] = ca[w];
+                J[NINT + w] = cb[w];
+              }
+              double s2;
+              h_double_ab<NINT>(a.t, my, J, &s2, nullptr, nullptr);
               const int64_t so = sout + scnt + __popc(sbal & lt);
               if (so < a.s2ptr[k + 1]) {
                 a.s2col[so] = jpos;
@@ -446,6 +434,59 @@ __global__ void __launch_bounds__(BLK) k_class_c(BuildArgs a) {
           a.s[k * a.nst + st] = sacc[st] + sd * uk;
         }
       }
+    }
+  }
+}
+
+// FP64 / FP32 elements of the stored pairs, after the fill pass has written
+// their columns: one warp per row, lanes over the row's pairs, so that the
+// dependent integral loads of 32 pairs are in flight at once (the fill's
+// scanning thread would evaluate its row's pairs one after the other).  The
+// class of a pair follows from the two determinants' strings, and each class
+// calls the same Slater routine with the same arguments as the scans do, so
+// the values are bit-identical.
+template <int NINT>
+__global__ void __launch_bounds__(BLK) k_pair_values(BuildArgs a) {
+  const int lane = threadIdx.x & 31;
+  const int64_t warp = ((int64_t)blockIdx.x * BLK + threadIdx.x) >> 5;
+  const int64_t nwarp = ((int64_t)gridDim.x * BLK) >> 5;
+  for (int64_t k = warp; k < a.N; k += nwarp) {
+    u64 my[2 * NINT];
+    const int bi = a.cols[k];
+#pragma unroll
+    for (int w = 0; w < NINT; ++w) {
+      my[w] = a.alpha_pos[k * NINT + w];
+      my[NINT + w] = a.beta[(int64_t)bi * NINT + w];
+    }
+    const int64_t e1 = a.rowptr[k + 1];
+    for (int64_t e = a.rowptr[k] + lane; e < e1; e += 32) {
+      const int j = a.colidx[e];
+      u64 J[2 * NINT];
+      const int bj = a.cols[j];
+      bool samea = true, sameb = true;
+      int da = 0, db = 0;
+#pragma unroll
+      for (int w = 0; w < NINT; ++w) {
+        J[w] = a.alpha_pos[(int64_t)j * NINT + w];
+        J[NINT + w] = a.beta[(int64_t)bj * NINT + w];
+        samea &= J[w] == my[w];
+        sameb &= J[NINT + w] == my[NINT + w];
+        da += popc64(my[w] ^ J[w]);
+        db += popc64(my[NINT + w] ^ J[NINT + w]);
+      }
+      double v;
+      if (sameb)  // class A (same beta column)
+        v = (da == 2) ? h_mono_spin<NINT>(a.t, my, J, 1, nullptr, nullptr)
+                      : h_double_spin<NINT>(a.t, my, J, nullptr, nullptr);
+      else if (samea)  // class B (same alpha row)
+        v = (db == 2) ? h_mono_spin<NINT>(a.t, my, J, 2, nullptr, nullptr)
+                      : h_double_spin<NINT>(a.t, my + NINT, J + NINT, nullptr, nullptr);
+      else {  // class C (alpha single x beta single)
+        double s2;
+        v = h_double_ab<NINT>(a.t, my, J, &s2, nullptr, nullptr);
+      }
+      a.val64[e] = v;
+      a.val32[e] = (float)v;
     }
   }
 }
@@ -592,6 +633,8 @@ int build_pairs_t(qpgpu_ctx* c) {
   qp_mark(c, "fill B");
   k_class_c<NINT, MODE_FILL><<<gC, BLK, 0, st>>>(a);
   qp_mark(c, "fill C");
+  k_pair_values<NINT><<<gC, BLK, 0, st>>>(a);
+  qp_mark(c, "pair elements");
   QP_CUDA(c, cudaGetLastError());
   int herr = 0;
   QP_CUDA(c, cudaMemcpyAsync(&herr, err.p, sizeof(int), cudaMemcpyDeviceToHost, st));
