@@ -22,6 +22,9 @@
 // compacts hits with __ballot_sync, scanning either the columns of the beta
 // singles of b (as the reference does) or the rows of the alpha singles of a,
 // whichever holds fewer determinants.
+#include <algorithm>
+#include <vector>
+
 #include <cub/cub.cuh>
 
 #include "qpgpu_internal.cuh"
@@ -75,7 +78,7 @@ struct BuildArgs {
   int* s2col;
   float* s2val;
   int* err;  // set when a fill pass would write past its row's segment
-  // direct sigma (MODE_SIGMA): v, s = H u, S^2 u for the selected rows, u (N, nst)
+  // direct sigma (k_pair_sigma): v, s = H u, S^2 u for the selected rows, u (N, nst)
   const double* u;
   const double* uT;  // u in alpha-major order: same-alpha partners are contiguous there
   double* v;
@@ -84,9 +87,18 @@ struct BuildArgs {
   const double* sdiag;
   int nst;
   int row_lo, row_hi, row_first, row_step;
+  // chunked direct sigma: the fill writes columns of rows [row_lo, row_hi) at
+  // rowptr[k] - col_base, class A blocks start at block blk_off, and same-alpha
+  // partners are written as alpha-major positions tagged with QP_TAG_T
+  int64_t col_base;
+  int64_t blk_off;
+  int write_s2;
+  int tag_t;
 };
 
-constexpr int MODE_COUNT = 0, MODE_FILL = 1, MODE_SIGMA = 2;
+constexpr unsigned QP_TAG_T = 0x80000000u;  // column given as alpha-major position
+
+constexpr int MODE_COUNT = 0, MODE_FILL = 1;
 
 __device__ __forceinline__ bool dsel(const BuildArgs& a, int64_t k) {
   return k >= a.row_lo && k < a.row_hi && ((k - a.row_first) % a.row_step) == 0;
@@ -109,9 +121,9 @@ __device__ __forceinline__ void dacc(const BuildArgs& a, double h, int64_t j, do
 // ---- class A: same beta column, alpha singles / doubles -------------------
 template <int NINT, int MODE>
 __global__ void __launch_bounds__(BLK) k_class_a(BuildArgs a) {
-  constexpr bool FILL = MODE == MODE_FILL, SIG = MODE == MODE_SIGMA;
+  constexpr bool FILL = MODE == MODE_FILL;
   __shared__ u64 tile[TILE * NINT];
-  const int64_t r0 = (int64_t)blockIdx.x * BLK;
+  const int64_t r0 = ((int64_t)blockIdx.x + a.blk_off) * BLK;
   if (r0 >= a.N) return;
   const int64_t k = r0 + threadIdx.x;
   const bool valid = k < a.N;
@@ -131,11 +143,10 @@ __global__ void __launch_bounds__(BLK) k_class_a(BuildArgs a) {
       my[w] = a.alpha[(int64_t)ai * NINT + w];
       my[NINT + w] = a.beta[(int64_t)b * NINT + w];
     }
-    if (FILL) out = a.rowptr[k];
+    if (FILL) out = a.rowptr[k] - a.col_base;
   }
   int cnt = 0;
-  double acc[8] = {0, 0, 0, 0, 0, 0, 0, 0};
-  const bool act = valid && (!SIG || dsel(a, k));
+  const bool act = valid && (MODE == MODE_COUNT || dsel(a, k));
   for (int t0 = U0; t0 < U1; t0 += TILE) {
     const int tn = min(TILE, U1 - t0);
     __syncthreads();
@@ -149,17 +160,7 @@ __global__ void __launch_bounds__(BLK) k_class_a(BuildArgs a) {
 #pragma unroll
         for (int w = 0; w < NINT; ++w) d += popc64(my[w] ^ c[w]);
         if (d == 2 || d == 4) {
-          if (SIG) {
-            u64 J[2 * NINT];
-#pragma unroll
-            for (int w = 0; w < NINT; ++w) {
-              J[w] = c[w];
-              J[NINT + w] = my[NINT + w];
-            }
-            const double v = (d == 2) ? h_mono_spin<NINT>(a.t, my, J, 1, nullptr, nullptr)
-                                      : h_double_spin<NINT>(a.t, my, c, nullptr, nullptr);
-            dacc(a, v, pos, acc);
-          } else if (FILL) {  // elements: k_pair_values
+          if (FILL) {  // elements: k_pair_values (stored) or k_pair_sigma (direct)
             if (cnt < a.cntA[k])
               a.colidx[out + cnt] = pos;
             else
@@ -171,14 +172,12 @@ __global__ void __launch_bounds__(BLK) k_class_a(BuildArgs a) {
     }
   }
   if (MODE == MODE_COUNT && valid) a.cntA[k] = cnt;
-  if (SIG && act)
-    for (int st = 0; st < a.nst; ++st) a.v[k * a.nst + st] = acc[st];
 }
 
 // ---- class B: same alpha row, beta singles / doubles ----------------------
 template <int NINT, int MODE>
 __global__ void __launch_bounds__(BLK) k_class_b(BuildArgs a) {
-  constexpr bool FILL = MODE == MODE_FILL, SIG = MODE == MODE_SIGMA;
+  constexpr bool FILL = MODE == MODE_FILL;
   __shared__ u64 tile[TILE * NINT];
   const int64_t q0 = (int64_t)blockIdx.x * BLK;
   if (q0 >= a.N) return;
@@ -200,11 +199,10 @@ __global__ void __launch_bounds__(BLK) k_class_b(BuildArgs a) {
       my[w] = a.alpha[(int64_t)ai * NINT + w];
       my[NINT + w] = a.beta[(int64_t)bi * NINT + w];
     }
-    if (FILL) out = a.rowptr[k] + a.cntA[k];
+    if (FILL) out = a.rowptr[k] + a.cntA[k] - a.col_base;
   }
   int cnt = 0;
-  double acc[8] = {0, 0, 0, 0, 0, 0, 0, 0};
-  const bool act = valid && (!SIG || dsel(a, k));
+  const bool act = valid && (MODE == MODE_COUNT || dsel(a, k));
   for (int t0 = V0; t0 < V1; t0 += TILE) {
     const int tn = min(TILE, V1 - t0);
     __syncthreads();
@@ -218,19 +216,9 @@ __global__ void __launch_bounds__(BLK) k_class_b(BuildArgs a) {
 #pragma unroll
         for (int w = 0; w < NINT; ++w) d += popc64(my[NINT + w] ^ c[w]);
         if (d == 2 || d == 4) {
-          if (SIG) {
-            u64 J[2 * NINT];
-#pragma unroll
-            for (int w = 0; w < NINT; ++w) {
-              J[w] = my[w];
-              J[NINT + w] = c[w];
-            }
-            const double v = (d == 2) ? h_mono_spin<NINT>(a.t, my, J, 2, nullptr, nullptr)
-                                      : h_double_spin<NINT>(a.t, my + NINT, c, nullptr, nullptr);
-            dacc_t(a, v, pos, acc);
-          } else if (FILL) {  // elements: k_pair_values
+          if (FILL) {  // elements: k_pair_values (stored) or k_pair_sigma (direct)
             if (cnt < a.cntB[k])
-              a.colidx[out + cnt] = a.t_order[pos];
+              a.colidx[out + cnt] = a.tag_t ? (int)(QP_TAG_T | (unsigned)pos) : a.t_order[pos];
             else
               atomicOr(a.err, 2);
           }
@@ -240,8 +228,6 @@ __global__ void __launch_bounds__(BLK) k_class_b(BuildArgs a) {
     }
   }
   if (MODE == MODE_COUNT && valid) a.cntB[k] = cnt;
-  if (SIG && act)
-    for (int st = 0; st < a.nst; ++st) a.v[k * a.nst + st] += acc[st];
 }
 
 // spin flip test of an alpha-single x beta-single pair: the two excitations
@@ -261,15 +247,14 @@ __device__ __forceinline__ bool spin_flip(const u64* my, const u64* ca, const u6
 // ---- class C: alpha single x beta single, one warp per row ----------------
 template <int NINT, int MODE>
 __global__ void __launch_bounds__(BLK) k_class_c(BuildArgs a) {
-  constexpr bool FILL = MODE == MODE_FILL, SIG = MODE == MODE_SIGMA;
+  constexpr bool FILL = MODE == MODE_FILL;
   const int lane = threadIdx.x & 31;
   const int64_t warp = ((int64_t)blockIdx.x * BLK + threadIdx.x) >> 5;
   const int64_t nwarp = ((int64_t)gridDim.x * BLK) >> 5;
   const unsigned lt = (1u << lane) - 1u;
   for (int64_t k = warp; k < a.N; k += nwarp) {
-    if (SIG && !dsel(a, k)) continue;
+    if (MODE != MODE_COUNT && !dsel(a, k)) continue;
     const int ai = a.rows[k], bi = a.cols[k];
-    double acc[8] = {0, 0, 0, 0, 0, 0, 0, 0}, sacc[8] = {0, 0, 0, 0, 0, 0, 0, 0};
     u64 my[2 * NINT];
 #pragma unroll
     for (int w = 0; w < NINT; ++w) {
@@ -278,7 +263,7 @@ __global__ void __launch_bounds__(BLK) k_class_c(BuildArgs a) {
     }
     int64_t out = 0, sout = 0;
     if (FILL) {
-      out = a.rowptr[k] + a.cntA[k] + a.cntB[k];
+      out = a.rowptr[k] + a.cntA[k] + a.cntB[k] - a.col_base;
       sout = a.s2ptr[k];
     }
     int cnt = 0, scnt = 0;
@@ -306,25 +291,13 @@ __global__ void __launch_bounds__(BLK) k_class_c(BuildArgs a) {
           const unsigned bal = __ballot_sync(0xffffffffu, hit);
           const bool flip = hit && spin_flip<NINT>(my, ca, cb);
           const unsigned sbal = __ballot_sync(0xffffffffu, flip);
-          if (SIG && hit) {
-            u64 J[2 * NINT];
-#pragma unroll
-            for (int w = 0; w < NINT; ++w) {
-              J[w] = ca[w];
-              J[NINT + w] = cb[w];
-            }
-            double s2;
-            const double v = h_double_ab<NINT>(a.t, my, J, &s2, nullptr, nullptr);
-            dacc(a, v, pos, acc);
-            if (flip) dacc(a, s2, pos, sacc);
-          }
           if (FILL && hit) {  // elements: k_pair_values; S^2 values of spin flips here
             const int64_t o = out + cnt + __popc(bal & lt);
-            if (o < a.rowptr[k + 1])
+            if (o < a.rowptr[k + 1] - a.col_base)
               a.colidx[o] = pos;
             else
               atomicOr(a.err, 4);
-            if (flip) {
+            if (flip && a.write_s2) {
               u64 J[2 * NINT];
 #pragma unroll
               for (int w = 0; w < NINT; ++w) {
@@ -369,26 +342,14 @@ __global__ void __launch_bounds__(BLK) k_class_c(BuildArgs a) {
           const unsigned bal = __ballot_sync(0xffffffffu, hit);
           const bool flip = hit && spin_flip<NINT>(my, ca, cb);
           const unsigned sbal = __ballot_sync(0xffffffffu, flip);
-          if (SIG && hit) {
-            u64 J[2 * NINT];
-#pragma unroll
-            for (int w = 0; w < NINT; ++w) {
-              J[w] = ca[w];
-              J[NINT + w] = cb[w];
-            }
-            double s2;
-            const double v = h_double_ab<NINT>(a.t, my, J, &s2, nullptr, nullptr);
-            dacc_t(a, v, q, acc);
-            if (flip) dacc_t(a, s2, q, sacc);
-          }
           if (FILL && hit) {  // elements: k_pair_values; S^2 values of spin flips here
             const int64_t o = out + cnt + __popc(bal & lt);
             const int jpos = a.t_order[q];
-            if (o < a.rowptr[k + 1])
-              a.colidx[o] = jpos;
+            if (o < a.rowptr[k + 1] - a.col_base)
+              a.colidx[o] = a.tag_t ? (int)(QP_TAG_T | (unsigned)q) : jpos;
             else
               atomicOr(a.err, 4);
-            if (flip) {
+            if (flip && a.write_s2) {
               u64 J[2 * NINT];
 #pragma unroll
               for (int w = 0; w < NINT; ++w) {
@@ -414,26 +375,6 @@ __global__ void __launch_bounds__(BLK) k_class_c(BuildArgs a) {
     if (MODE == MODE_COUNT && lane == 0) {
       a.cntC[k] = cnt;
       a.cntS[k] = scnt;
-    }
-    if (SIG) {
-      // lanes combined in a fixed butterfly order; lane 0 finishes the row
-#pragma unroll
-      for (int st = 0; st < 8; ++st) {
-        if (st >= a.nst) break;
-#pragma unroll
-        for (int o = 16; o > 0; o >>= 1) {
-          acc[st] += __shfl_xor_sync(0xffffffffu, acc[st], o);
-          sacc[st] += __shfl_xor_sync(0xffffffffu, sacc[st], o);
-        }
-      }
-      if (lane == 0) {
-        const double hd = a.hdiag[k], sd = a.sdiag[k];
-        for (int st = 0; st < a.nst; ++st) {
-          const double uk = a.u[k * a.nst + st];
-          a.v[k * a.nst + st] = (a.v[k * a.nst + st] + acc[st]) + hd * uk;
-          a.s[k * a.nst + st] = sacc[st] + sd * uk;
-        }
-      }
     }
   }
 }
@@ -543,6 +484,10 @@ BuildArgs index_args(const qpgpu_ctx* c) {
   a.row_hi = (int)c->N;
   a.row_first = 0;
   a.row_step = 1;
+  a.col_base = 0;
+  a.blk_off = 0;
+  a.write_s2 = 1;
+  a.tag_t = 0;
   return a;
 }
 
@@ -598,6 +543,15 @@ int build_pairs_t(qpgpu_ctx* c) {
   }
   c->direct = direct;
   if (direct) {
+    // the direct sigma regenerates the columns chunk by chunk: keep the
+    // per-row counts of the same-spin classes and the row starts on the host
+    c->d_cntA = cA.p;
+    cA.p = nullptr;
+    c->d_cntB = cB.p;
+    cB.p = nullptr;
+    c->h_rowptr.resize(N + 1);
+    QP_CUDA(c, cudaMemcpyAsync(c->h_rowptr.data(), c->d_rowptr, (N + 1) * sizeof(int64_t), cudaMemcpyDeviceToHost,
+                               st));
     QP_CUDA(c, dev_alloc(&c->d_hdiag, N));
     QP_CUDA(c, dev_alloc(&c->d_sdiag, N));
     QP_CUDA(c, dev_alloc(&c->d_hdiag32, N));
@@ -656,9 +610,89 @@ __global__ void k_alpha_major(const double* u, const int* t_order, double* uT, i
     uT[t] = u[(int64_t)t_order[t / nst] * nst + t % nst];
 }
 
+// Direct sigma of the rows [row_lo, row_hi) of one chunk, after the fill
+// scans wrote their columns into pc (at rowptr[k] - col_base): one warp per
+// row, lanes over its pairs; each pair's element is evaluated as in
+// k_pair_values (same routines, same arguments), multiplied by the partner's
+// coefficients (same-alpha partners, tagged with their alpha-major position,
+// read from the alpha-major copy uT, where a row's partners are contiguous),
+// and the lanes are combined in a fixed butterfly order.
 template <int NINT>
-void sigma_direct_t(qpgpu_ctx* c, double* v, double* s, const double* u, const double* uT, int nst,
-                    cudaStream_t st, int row_lo, int row_hi, int row_first, int row_step) {
+__global__ void __launch_bounds__(BLK) k_pair_sigma(BuildArgs a, const int* __restrict__ pc) {
+  const int lane = threadIdx.x & 31;
+  const int64_t warp = ((int64_t)blockIdx.x * BLK + threadIdx.x) >> 5;
+  const int64_t nwarp = ((int64_t)gridDim.x * BLK) >> 5;
+  for (int64_t k = a.row_lo + warp; k < a.row_hi; k += nwarp) {
+    if (((k - a.row_first) % a.row_step) != 0) continue;
+    u64 my[2 * NINT];
+    const int bi = a.cols[k];
+#pragma unroll
+    for (int w = 0; w < NINT; ++w) {
+      my[w] = a.alpha_pos[k * NINT + w];
+      my[NINT + w] = a.beta[(int64_t)bi * NINT + w];
+    }
+    double acc[8] = {0, 0, 0, 0, 0, 0, 0, 0}, sacc[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+    const int64_t e1 = a.rowptr[k + 1];
+    for (int64_t e = a.rowptr[k] + lane; e < e1; e += 32) {
+      const unsigned cj = (unsigned)pc[e - a.col_base];
+      const bool via_t = (cj & QP_TAG_T) != 0;
+      const int q = (int)(cj & ~QP_TAG_T);
+      const int j = via_t ? a.t_order[q] : q;
+      u64 J[2 * NINT];
+      const int bj = a.cols[j];
+      bool samea = true, sameb = true;
+      int da = 0, db = 0;
+#pragma unroll
+      for (int w = 0; w < NINT; ++w) {
+        J[w] = a.alpha_pos[(int64_t)j * NINT + w];
+        J[NINT + w] = a.beta[(int64_t)bj * NINT + w];
+        samea &= J[w] == my[w];
+        sameb &= J[NINT + w] == my[NINT + w];
+        da += popc64(my[w] ^ J[w]);
+        db += popc64(my[NINT + w] ^ J[NINT + w]);
+      }
+      double v, s2 = 0.0;
+      if (sameb)
+        v = (da == 2) ? h_mono_spin<NINT>(a.t, my, J, 1, nullptr, nullptr)
+                      : h_double_spin<NINT>(a.t, my, J, nullptr, nullptr);
+      else if (samea)
+        v = (db == 2) ? h_mono_spin<NINT>(a.t, my, J, 2, nullptr, nullptr)
+                      : h_double_spin<NINT>(a.t, my + NINT, J + NINT, nullptr, nullptr);
+      else
+        v = h_double_ab<NINT>(a.t, my, J, &s2, nullptr, nullptr);
+      if (via_t) {
+        dacc_t(a, v, q, acc);
+        if (s2 != 0.0) dacc_t(a, s2, q, sacc);
+      } else {
+        dacc(a, v, j, acc);
+        if (s2 != 0.0) dacc(a, s2, j, sacc);
+      }
+    }
+#pragma unroll
+    for (int st = 0; st < 8; ++st) {
+      if (st >= a.nst) break;
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) {
+        acc[st] += __shfl_xor_sync(0xffffffffu, acc[st], o);
+        sacc[st] += __shfl_xor_sync(0xffffffffu, sacc[st], o);
+      }
+    }
+    if (lane == 0) {
+      const double hd = a.hdiag[k], sd = a.sdiag[k];
+      for (int st = 0; st < a.nst; ++st) {
+        const double uk = a.u[k * a.nst + st];
+        a.v[k * a.nst + st] = acc[st] + hd * uk;
+        a.s[k * a.nst + st] = sacc[st] + sd * uk;
+      }
+    }
+  }
+}
+
+// chunks of rows whose columns fit the buffer: fill scans restricted to the
+// chunk (S^2 lists not written), then k_pair_sigma
+template <int NINT>
+int sigma_direct_t(qpgpu_ctx* c, double* v, double* s, const double* u, const double* uT, int nst,
+                   cudaStream_t st, int row_lo, int row_hi, int row_first, int row_step) {
   BuildArgs a = index_args(c);
   a.u = u;
   a.uT = uT;
@@ -667,15 +701,42 @@ void sigma_direct_t(qpgpu_ctx* c, double* v, double* s, const double* u, const d
   a.hdiag = c->d_hdiag;
   a.sdiag = c->d_sdiag;
   a.nst = nst;
-  a.row_lo = row_lo;
-  a.row_hi = row_hi;
+  a.rowptr = c->d_rowptr;
+  a.s2ptr = c->d_s2ptr;
+  a.cntA = c->d_cntA;
+  a.cntB = c->d_cntB;
+  a.colidx = c->d_direct_cols;
+  a.err = c->d_direct_err;
+  a.write_s2 = 0;
+  a.tag_t = 1;
   a.row_first = row_first;
   a.row_step = row_step;
-  const unsigned gAB = nblocks(c->N, BLK);
-  const unsigned gC = nblocks(c->N * 32, BLK);
-  k_class_a<NINT, MODE_SIGMA><<<gAB, BLK, 0, st>>>(a);
-  k_class_b<NINT, MODE_SIGMA><<<gAB, BLK, 0, st>>>(a);
-  k_class_c<NINT, MODE_SIGMA><<<gC, BLK, 0, st>>>(a);
+  const int64_t N = c->N;
+  const std::vector<int64_t>& rp = c->h_rowptr;
+  const unsigned gAB = nblocks(N, BLK);
+  const unsigned gC = nblocks(N * 32, BLK);
+  int64_t clo = 0;
+  while (clo < N) {
+    // largest chi with rp[chi] - rp[clo] <= capacity (at least one row)
+    const int64_t lim = rp[clo] + c->direct_cols_cap;
+    int64_t chi = std::upper_bound(rp.begin() + clo + 1, rp.end(), lim) - rp.begin() - 1;
+    if (chi <= clo) chi = clo + 1;
+    const int64_t lo = std::max<int64_t>(clo, row_lo), hi = std::min<int64_t>(chi, row_hi);
+    if (lo < hi) {
+      a.row_lo = (int)lo;
+      a.row_hi = (int)hi;
+      a.col_base = rp[lo];
+      a.blk_off = lo / BLK;
+      const unsigned gA = (unsigned)((hi - 1) / BLK - lo / BLK + 1);
+      k_class_a<NINT, MODE_FILL><<<gA, BLK, 0, st>>>(a);
+      k_class_b<NINT, MODE_FILL><<<gAB, BLK, 0, st>>>(a);
+      k_class_c<NINT, MODE_FILL><<<gC, BLK, 0, st>>>(a);
+      k_pair_sigma<NINT><<<nblocks((hi - lo) * 32, BLK), BLK, 0, st>>>(a, c->d_direct_cols);
+    }
+    clo = chi;
+  }
+  QP_CUDA(c, cudaGetLastError());
+  return 0;
 }
 
 }  // namespace
@@ -694,11 +755,26 @@ int qp_sigma_direct(qpgpu_ctx* c, double* v, double* s, const double* u, int nst
     QP_CUDA(c, dev_alloc(&c->d_direct_ut, need));
     c->direct_ut_n = need;
   }
+  if (!c->d_direct_cols) {  // column buffer: the whole set if it fits in half the free memory
+    size_t fr = 0, total = 0;
+    QP_CUDA(c, cudaMemGetInfo(&fr, &total));
+    int64_t maxrow = 0;
+    for (int64_t k = 0; k < c->N; ++k) maxrow = std::max(maxrow, c->h_rowptr[k + 1] - c->h_rowptr[k]);
+    int64_t cap = std::min<int64_t>(c->P, (int64_t)(fr / 2 / sizeof(int)));
+    // QPGPU_DIRECT_CHUNK_COLS caps the buffer (a memory budget; small values
+    // force many chunks)
+    if (const char* e = getenv("QPGPU_DIRECT_CHUNK_COLS")) cap = std::min<int64_t>(cap, atoll(e) > 0 ? atoll(e) : cap);
+    cap = std::max<int64_t>(cap, maxrow);
+    QP_CUDA(c, dev_alloc(&c->d_direct_cols, (size_t)std::max<int64_t>(cap, 1)));
+    QP_CUDA(c, dev_alloc(&c->d_direct_err, 1));
+    QP_CUDA(c, cudaMemsetAsync(c->d_direct_err, 0, sizeof(int), st));
+    c->direct_cols_cap = cap;
+  }
   k_alpha_major<<<nblocks((int64_t)need, 256), 256, 0, st>>>(u, c->d_t_order, c->d_direct_ut, c->N, nst);
-  if (c->nint == 1)
-    sigma_direct_t<1>(c, v, s, u, c->d_direct_ut, nst, st, row_lo, row_hi, row_first, row_step);
-  else
-    sigma_direct_t<2>(c, v, s, u, c->d_direct_ut, nst, st, row_lo, row_hi, row_first, row_step);
+  const int rc = (c->nint == 1)
+                     ? sigma_direct_t<1>(c, v, s, u, c->d_direct_ut, nst, st, row_lo, row_hi, row_first, row_step)
+                     : sigma_direct_t<2>(c, v, s, u, c->d_direct_ut, nst, st, row_lo, row_hi, row_first, row_step);
+  if (rc) return rc;
   QP_CUDA(c, cudaGetLastError());
   return 0;
 }
@@ -714,6 +790,13 @@ void qp_free_pairs(qpgpu_ctx* c) {
   }
   c->have_pairs = false;
   c->direct = false;
+  void** dp[] = {(void**)&c->d_cntA, (void**)&c->d_cntB, (void**)&c->d_direct_cols, (void**)&c->d_direct_err};
+  for (auto p : dp) {
+    dev_free(*p);
+    *p = nullptr;
+  }
+  c->direct_cols_cap = 0;
+  c->h_rowptr.clear();
   c->P = c->P_s2 = 0;
 }
 

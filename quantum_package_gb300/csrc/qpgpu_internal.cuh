@@ -399,6 +399,12 @@ struct qpgpu_ctx {
   bool direct = false;                // pairs not stored: sigma enumerates them (pairs.cu)
   double* d_direct_ut = nullptr;      // direct sigma: u in alpha-major order
   size_t direct_ut_n = 0;
+  int* d_cntA = nullptr;              // direct sigma: same-beta / same-alpha pairs per row
+  int* d_cntB = nullptr;
+  std::vector<int64_t> h_rowptr;      // direct sigma: row starts (host)
+  int* d_direct_cols = nullptr;       // direct sigma: columns of one chunk of rows
+  int64_t direct_cols_cap = 0;
+  int* d_direct_err = nullptr;
   int64_t P = 0;
   int64_t* d_rowptr = nullptr;  // N+1
   int* d_colidx = nullptr;      // P

@@ -90,3 +90,17 @@ def test_stored_pair_entry_points_refuse_direct_sets(pair):
     p, stored, direct = pair
     with pytest.raises(QPGPUError):
         direct.connected_pairs()
+
+
+def test_direct_sigma_in_many_chunks(monkeypatch):
+    # the direct sigma regenerates the columns chunk by chunk; a small column
+    # budget forces hundreds of chunks, with the same results
+    from quantum_package_gb300.sigma import Wavefunction
+    p = G.make_problem(2, n_det=3000)
+    monkeypatch.setenv("QPGPU_DIRECT_CHUNK_COLS", "7")
+    direct = Wavefunction.from_problem(p, sigma_mode=SIGMA_DIRECT)
+    u = G.random_coefficients(p.n_det, 3, p.seed)
+    vd, sd = direct.H_S2_u_0_nstates_openmp(u)
+    monkeypatch.delenv("QPGPU_DIRECT_CHUNK_COLS")
+    vo, so = Oracle.from_problem(p).h_s2_u0(u)
+    assert _rel(vd, vo) <= REL64 and _rel(sd, so) <= REL64
