@@ -521,9 +521,33 @@ __global__ void __launch_bounds__(DBLK) k_step(double* Un, const double* Wn, con
   }
 }
 
+// Features of the target states for the learned step (qp_features), one row
+// of QP_MLP_IN floats per (determinant, state); the network is evaluated on
+// them by qp_mlp_eval (a spill-free inference kernel) before k_step_mlp.
+__global__ void __launch_bounds__(DBLK) k_mlp_features(const double* Un, const double* Wn, const double* Sn,
+                                                        const double* hjj, const float4* feat, int64_t N, StepParams p,
+                                                        float* X) {
+  for (int64_t r = blockIdx.x * (int64_t)DBLK + threadIdx.x; r < N; r += (int64_t)gridDim.x * DBLK) {
+    const double h = hjj[r];
+    const float4 st = feat[r];
+    for (int k = 0; k < p.nst; ++k) {
+      const int64_t x = r * p.nsd + k;
+      const double u = Un[x];
+      const double res = p.lambda[k] * u - Wn[x];
+      const double d = res * (1.0 + p.s2[k] * u - Sn[x] - p.sz2sz) / fmax(h - p.lambda[k], 1e-2);
+      float f[QP_MLP_IN];
+      qp_features(st, h - p.lambda[k], u, res, d, f);
+      float* o = X + (r * p.nst + k) * QP_MLP_IN;
+#pragma unroll
+      for (int i = 0; i < QP_MLP_IN; ++i) o[i] = f[i];
+    }
+  }
+}
+
 // Davidson step with the learned preconditioner.  d_k is the reference's
 // diagonal correction of Ritz vector k (its squared norm stays the
-// convergence measure); g_k the MLP's per-determinant multiplier.
+// convergence measure); g_k = G[r * nst + k] the MLP's per-determinant
+// multiplier.
 //   replace (extra == 0): state k flagged in mlp_mask takes g_k d_k instead
 //     of d_k;
 //   extra (extra == 1): the correction slot of the non-target Ritz vector
@@ -532,18 +556,14 @@ __global__ void __launch_bounds__(DBLK) k_step(double* Un, const double* Wn, con
 //     poor network costs a little of the block's extra directions instead of
 //     the target's own step.
 __global__ void __launch_bounds__(DBLK) k_step_mlp(double* Un, const double* Wn, const double* Sn, const double* hjj,
-                                                   const float4* feat, const float* P, int64_t N, StepParams p,
-                                                   unsigned mlp_mask, int extra, double* partial) {
-  __shared__ float Ps[QP_MLP_NPARAM];
+                                                   const float* G, int64_t N, StepParams p, unsigned mlp_mask,
+                                                   int extra, double* partial) {
   __shared__ double red[MAXS][DBLK / 32];
-  for (int i = threadIdx.x; i < QP_MLP_NPARAM; i += DBLK) Ps[i] = P[i];
-  __syncthreads();
   double acc[MAXS];
 #pragma unroll
   for (int k = 0; k < MAXS; ++k) acc[k] = 0.0;
   for (int64_t r = blockIdx.x * (int64_t)DBLK + threadIdx.x; r < N; r += (int64_t)gridDim.x * DBLK) {
     const double h = hjj[r];
-    const float4 st = feat[r];
     double learned[MAXS];  // g_k d_k of the flagged target states (extra mode)
 #pragma unroll
     for (int k = 0; k < MAXS; ++k) {
@@ -555,9 +575,7 @@ __global__ void __launch_bounds__(DBLK) k_step_mlp(double* Un, const double* Wn,
       const double d = res * (1.0 + p.s2[k] * u - Sn[x] - p.sz2sz) / fmax(h - p.lambda[k], 1e-2);
       double v = d;
       if (k < p.nst && ((mlp_mask >> k) & 1u)) {
-        float f[QP_MLP_IN];
-        qp_features(st, h - p.lambda[k], u, res, d, f);
-        const double gd = d * (double)qp_mlp_forward(Ps, f);
+        const double gd = d * (double)G[r * p.nst + k];
         if (extra)
           learned[k] = gd;
         else
@@ -692,6 +710,7 @@ struct Dav {
   double* part = nullptr;  // gram / step partials
   double* small = nullptr;  // device small matrices (MAXM*MAXS x 6)
   float *cX = nullptr, *cd = nullptr, *cc = nullptr;  // training capture
+  float *mlpX = nullptr, *mlpG = nullptr;              // learned step: features, multipliers
   int ncta = 0;
   int64_t rows_per_cta = 0;
   ~Dav() {
@@ -705,6 +724,8 @@ struct Dav {
     dev_free(cX);
     dev_free(cd);
     dev_free(cc);
+    dev_free(mlpX);
+    dev_free(mlpG);
   }
   double* blk(double* X, int b) const { return X + (int64_t)b * N * nsd; }
 };
@@ -931,6 +952,11 @@ extern "C" int qpgpu_davidson_hs2(qpgpu_ctx* c, double* u_in, int64_t dim_in, do
   // extra mode: state k's learned correction uses the slot of Ritz vector nst + k
   const int mlp_extra = prm->preconditioner == 2;
   for (int k = 0; k < nst; ++k) mlp_on[k] = use_mlp && (!mlp_extra || nst + k < nsd);
+  if (use_mlp && (dev_alloc(&d.mlpX, (size_t)N * nst * QP_MLP_IN) != cudaSuccess ||
+                  dev_alloc(&d.mlpG, (size_t)N * nst) != cudaSuccess)) {
+    cudaGetLastError();
+    return qpgpu_fail(c, QPGPU_ERR_NOMEM, "learned-step work arrays do not fit on the device");
+  }
   int n_fallback = 0;
   const int collect_every = prm->collect_every > 0 ? prm->collect_every : 0;
   const int collect_max = collect_every ? std::max(1, std::min(prm->collect_max > 0 ? prm->collect_max : 8, 64 / nst)) : 0;
@@ -1086,9 +1112,13 @@ extern "C" int qpgpu_davidson_hs2(qpgpu_ctx* c, double* u_in, int64_t dim_in, do
       unsigned mask = 0;
       for (int k = 0; k < nst; ++k)
         if (mlp_on[k]) mask |= 1u << k;
-      if (mask)
-        k_step_mlp<<<d.ncta, DBLK, 0, st>>>(d.blk(d.U, iter), d.blk(d.W, iter), d.blk(d.S, iter), c->d_hdiag,
-                                            (const float4*)c->d_detfeat, c->mlp.params, N, sp, mask, mlp_extra, d.part);
+      if (mask) {
+        k_mlp_features<<<gsz(N), DBLK, 0, st>>>(d.blk(d.U, iter), d.blk(d.W, iter), d.blk(d.S, iter), c->d_hdiag,
+                                                (const float4*)c->d_detfeat, N, sp, d.mlpX);
+        qp_mlp_eval(c->mlp.params, d.mlpX, d.mlpG, N * nst, st);
+        k_step_mlp<<<d.ncta, DBLK, 0, st>>>(d.blk(d.U, iter), d.blk(d.W, iter), d.blk(d.S, iter), c->d_hdiag, d.mlpG,
+                                            N, sp, mask, mlp_extra, d.part);
+      }
       else
         k_step<<<d.ncta, DBLK, 0, st>>>(d.blk(d.U, iter), d.blk(d.W, iter), d.blk(d.S, iter), c->d_hdiag, N, sp, d.part);
       QP_CUDA(c, cudaGetLastError());

@@ -170,7 +170,7 @@ __global__ void k_mlp_reduce_adam(const float* partial, int ncta, int nb, float*
 }
 
 __global__ void __launch_bounds__(256) k_mlp_predict(const float* P, const float* X, float* y, int64_t n) {
-  __shared__ float Ps[QP_MLP_NPARAM];
+  __shared__ __align__(16) float Ps[QP_MLP_NPARAM];
   for (int i = threadIdx.x; i < QP_MLP_NPARAM; i += blockDim.x) Ps[i] = P[i];
   __syncthreads();
   for (int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; q < n; q += (int64_t)gridDim.x * blockDim.x) {
@@ -179,6 +179,16 @@ __global__ void __launch_bounds__(256) k_mlp_predict(const float* P, const float
     y[q] = qp_mlp_forward(Ps, f);
   }
 }
+
+}  // namespace
+
+// y[q] = MLP(X[q]) for n samples (inference of the learned Davidson step)
+void qp_mlp_eval(const float* P, const float* X, float* y, int64_t n, cudaStream_t st) {
+  const int64_t g = std::min<int64_t>(gsz(n), 152 * 8);
+  k_mlp_predict<<<(unsigned)std::max<int64_t>(g, 1), 256, 0, st>>>(P, X, y, n);
+}
+
+namespace {
 
 int ensure_mlp(qpgpu_ctx* c) {
   if (c->mlp.params) return 0;

@@ -490,6 +490,7 @@ void qp_report_marks(qpgpu_ctx* c);  // ctx.cu
 // learned preconditioner (mlp.cu)
 int qp_det_features(qpgpu_ctx* c);
 int qp_mlp_append(qpgpu_ctx* c, const float* X, const float* G, const float* W, int64_t n, bool device_src);
+void qp_mlp_eval(const float* P, const float* X, float* y, int64_t n, cudaStream_t st);
 #ifdef __CUDACC__
 __device__ __forceinline__ float qp_gelu(float x) { return 0.5f * x * (1.0f + erff(x * 0.70710678118654752f)); }
 __device__ __forceinline__ float qp_gelu_grad(float x) {
@@ -506,21 +507,37 @@ __device__ __forceinline__ void qp_features(const float4 st, double hmL, double 
   f[6] = (float)(log10(fabs(r) + 1e-30) / 8.0);
   f[7] = (float)(log10(fabs(d) + 1e-30) / 8.0);
 }
-// forward pass with the parameters in shared memory
+// forward pass with the parameters in shared memory (P 16-byte aligned: the
+// weight rows start at multiples of 4 floats, so each 16-byte broadcast load
+// feeds four FMAs; the summation order is that of the plain loops)
+static_assert(QP_MLP_W1 % 4 == 0 && QP_MLP_W2 % 4 == 0 && QP_MLP_IN % 4 == 0 && QP_MLP_H % 4 == 0,
+              "MLP weight rows must be 16-byte aligned");
 __device__ __forceinline__ float qp_mlp_forward(const float* P, const float* f) {
-  float h1[QP_MLP_H];
-#pragma unroll 8
+  float h1[QP_MLP_H];  // fully unrolled below, so it stays in registers
+#pragma unroll
   for (int j = 0; j < QP_MLP_H; ++j) {
     float a = P[QP_MLP_B1 + j];
 #pragma unroll
-    for (int i = 0; i < QP_MLP_IN; ++i) a = fmaf(P[QP_MLP_W1 + j * QP_MLP_IN + i], f[i], a);
+    for (int i = 0; i < QP_MLP_IN; i += 4) {
+      const float4 w = *reinterpret_cast<const float4*>(&P[QP_MLP_W1 + j * QP_MLP_IN + i]);
+      a = fmaf(w.x, f[i], a);
+      a = fmaf(w.y, f[i + 1], a);
+      a = fmaf(w.z, f[i + 2], a);
+      a = fmaf(w.w, f[i + 3], a);
+    }
     h1[j] = qp_gelu(a);
   }
   float y = P[QP_MLP_B3];
   for (int j = 0; j < QP_MLP_H; ++j) {
     float a = P[QP_MLP_B2 + j];
-#pragma unroll 16
-    for (int i = 0; i < QP_MLP_H; ++i) a = fmaf(P[QP_MLP_W2 + j * QP_MLP_H + i], h1[i], a);
+#pragma unroll
+    for (int i = 0; i < QP_MLP_H; i += 4) {
+      const float4 w = *reinterpret_cast<const float4*>(&P[QP_MLP_W2 + j * QP_MLP_H + i]);
+      a = fmaf(w.x, h1[i], a);
+      a = fmaf(w.y, h1[i + 1], a);
+      a = fmaf(w.z, h1[i + 2], a);
+      a = fmaf(w.w, h1[i + 3], a);
+    }
     y = fmaf(P[QP_MLP_W3 + j], qp_gelu(a), y);
   }
   return y;
