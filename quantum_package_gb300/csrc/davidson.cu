@@ -22,6 +22,11 @@
 // restart, so the reported energies and residuals are FP64 ones.  With
 // QPGPU_FF the restart sigma is the float-float one (k_sigma_ff, FP64-class
 // accuracy on the FP32 pipes) and convergence is accepted on those iterations.
+// In both mixed modes the tall-skinny algebra (Gram blocks of the
+// Gram-Schmidt passes and projections, the updates, Ritz vectors and
+// re-contraction) runs in float-float on the FP32 pipes (k_gram<., true>,
+// k_lincomb_ff); the small factorisations, the eigenproblem, the step and
+// the residual norms stay FP64.
 #include <algorithm>
 #include <cmath>
 #include <cstring>
@@ -165,6 +170,29 @@ inline unsigned gsz(int64_t n, int tpb = DBLK) {
   return (unsigned)g;
 }
 
+// hi + lo += x * y for split operands x = xh + xl, y = yh + yl: the product
+// of the high parts exactly (rounded value plus its FMA error), the two cross
+// terms (the lo * lo term is below 2^-46 of the product), and Knuth's TwoSum
+// on the high part of the running sum
+__device__ __forceinline__ void ff_mac(float& hi, float& lo, float xh, float xl, float yh, float yl) {
+  const float p = __fmul_rn(xh, yh);
+  float pe = __fmaf_rn(xh, yh, -p);
+  pe = __fmaf_rn(xh, yl, pe);
+  pe = __fmaf_rn(xl, yh, pe);
+  float s, e;
+  qpsig::two_sum(hi, p, s, e);
+  hi = s;
+  lo = __fadd_rn(lo, __fadd_rn(e, pe));
+}
+
+// moves what the low part has gathered into the high part (Dekker's
+// Fast2Sum; |lo| <= |hi| up to the rounding of the accumulated errors)
+__device__ __forceinline__ void ff_renorm(float& hi, float& lo) {
+  const float s = __fadd_rn(hi, lo);
+  lo = __fsub_rn(lo, __fsub_rn(s, hi));
+  hi = s;
+}
+
 // G[i][j] = sum_r A_i[r] B_j[r]: A has m columns (column i is column i % nsd
 // of the block i / nsd; blocks strideA apart, rows of nsd values), B is B0
 // (nsd columns) or [B0 B1] (2 nsd columns), NBC = the number of B columns.
@@ -246,6 +274,166 @@ __global__ void k_reduce_partials(const double* partial, int ncta, int np, doubl
   }
 }
 
+// Float-float copies of Davidson blocks for the mixed-precision Gram blocks:
+// out[r][j] = split of X0[r][j] (j < nsd) or X1[r][j - nsd] (nx = 2), so a
+// row of out holds nx * nsd (hi, lo) pairs.  Every operand of k_gram_ff is
+// split once here instead of once per use.
+__global__ void k_split_block(const double* __restrict__ X0, const double* __restrict__ X1, int nsd, int nx,
+                              int64_t N, float2* __restrict__ out, const int* skip) {
+  if (skip && *skip) return;
+  // flat over the nsd * N elements of each source block (coalesced loads and
+  // stores); the row of element i is i / nsd (32-bit when it fits)
+  const int64_t n = N * nsd;
+  const bool small = n < (1LL << 31);
+  for (int t = 0; t < nx; ++t) {
+    const double* x = t ? X1 : X0;
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+      float h, l;
+      qpsig::split_ff(x[i], h, l);
+      int64_t o = i;
+      if (nx > 1) {
+        const int64_t r = small ? (int64_t)((unsigned)i / (unsigned)nsd) : i / nsd;
+        o = r * (nx * nsd) + t * nsd + (i - r * nsd);
+      }
+      out[o] = make_float2(h, l);
+    }
+  }
+}
+
+// k_gram in float-float arithmetic on the FP32 pipes (GB300: 64 FP32 FMAs per
+// FP64 FMA), for the mixed-precision Davidson's Gram-Schmidt passes and
+// projections.  A = m split columns (consecutive split blocks of nsd, block
+// stride sA), B = N rows of NBC split values (k_split_block).  The CTA tiling
+// over rows and column groups is k_gram's, but each lane owns one entry
+// (q, j) = (lane / NBC, lane % NBC) of its warp's CI x NBC tile and runs over
+// the rows: tiles of T rows of the CTA's A blocks and of B are staged in
+// shared memory by cp.async (double-buffered), and a lane reads one A and one
+// B value per row as conflict-free broadcasts.  Each product is ff_mac (about
+// 47 bits), the pairs are renormalised every 16 rows, warps of a column group
+// and CTAs are combined in FP64 in a fixed order (deterministic sums).
+__device__ __forceinline__ void cp_async8(void* sdst, const void* gsrc) {
+  const unsigned sa = (unsigned)__cvta_generic_to_shared(sdst);
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 8;\n" ::"r"(sa), "l"(gsrc) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
+__device__ __forceinline__ void cp_async_wait1() { asm volatile("cp.async.wait_group 1;\n" ::: "memory"); }
+
+struct GramTile {
+  int k_lo, nblk;
+};
+// the split blocks that hold the columns [cg0 * ci, min(m, (cg0 + ncg_here) * ci))
+// of gridDim.y slice cgy
+__host__ __device__ inline GramTile gram_tile(int m, int nsd, int nbc, int cgy) {
+  const int ci = 32 / nbc;
+  const int ncg = (m + ci - 1) / ci;
+  const int cg0 = cgy * (DBLK / 32);
+  const int ncg_here = ncg - cg0 < DBLK / 32 ? ncg - cg0 : DBLK / 32;
+  const int c_lo = cg0 * ci, c_hi = m < (cg0 + ncg_here) * ci ? m : (cg0 + ncg_here) * ci;
+  GramTile g;
+  g.k_lo = c_lo / nsd;
+  g.nblk = (c_hi - 1) / nsd - g.k_lo + 1;
+  return g;
+}
+// widest staged row (float2) over the gridDim.y slices, and the row-tile
+// height T: two stages in about 72 KB, so three CTAs share an SM
+inline int gram_stage_width(int m, int nsd, int nbc) {
+  const int ci = 32 / nbc;
+  const int ny = ((m + ci - 1) / ci + DBLK / 32 - 1) / (DBLK / 32);
+  int w = 0;
+  for (int y = 0; y < ny; ++y) w = std::max(w, gram_tile(m, nsd, nbc, y).nblk * nsd + nbc);
+  return w;
+}
+inline int gram_rows_per_stage(int width) {
+  const int T = (72 * 1024 / (2 * (int)sizeof(float2) * width)) / 32 * 32;
+  return std::max(32, std::min(T, 256));
+}
+
+template <int NBC, int NSD>
+__global__ void __launch_bounds__(DBLK) k_gram_ff(const float2* __restrict__ A, int m, int64_t sA,
+                                                  const float2* __restrict__ B, int64_t N, int64_t rows_per_cta,
+                                                  int T, double* partial, const int* skip) {
+  constexpr int CI = 32 / NBC;
+  if (skip && *skip) return;
+  extern __shared__ float2 stage[];
+  __shared__ double red[DBLK / 32][32];
+  const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int ncg = (m + CI - 1) / CI;
+  const int cg0 = blockIdx.y * (DBLK / 32);
+  const int ncg_here = min(DBLK / 32, ncg - cg0);
+  const int rg = (DBLK / 32) / ncg_here;
+  const int cgl = w % ncg_here, rgi = w / ncg_here;
+  const bool active = rgi < rg;
+  const GramTile gt = gram_tile(m, NSD, NBC, blockIdx.y);
+  const int wA = gt.nblk * NSD;                 // A float2 per staged row
+  const int64_t ssz = (int64_t)T * (wA + NBC);  // float2 per stage
+  // this lane's entry
+  const int q = lane / NBC, j = lane % NBC;
+  const int col = (cg0 + cgl) * CI + q;
+  const bool mine = active && q < CI && col < m;
+  const int cc = mine ? col : gt.k_lo * NSD;
+  const int aoff = (cc / NSD - gt.k_lo) * T * NSD + (cc % NSD);  // within the A part of a stage
+  const int64_t r0 = (int64_t)blockIdx.x * rows_per_cta;
+  const int64_t r1 = min(r0 + rows_per_cta, N);
+  auto issue = [&](int64_t r, float2* buf) {
+    const int nr = (int)min((int64_t)T, r1 - r);
+    for (int kb = 0; kb < gt.nblk; ++kb) {
+      const float2* src = A + (int64_t)(gt.k_lo + kb) * sA + r * NSD;
+      float2* dst = buf + kb * T * NSD;
+      for (int e = threadIdx.x; e < nr * NSD; e += DBLK) cp_async8(dst + e, src + e);
+    }
+    const float2* src = B + r * NBC;
+    float2* dst = buf + T * wA;
+    for (int e = threadIdx.x; e < nr * NBC; e += DBLK) cp_async8(dst + e, src + e);
+  };
+  // a warp takes a contiguous share of each staged tile; two accumulator
+  // pairs (alternate rows) give its in-order issue two independent TwoSum
+  // chains, and strides are compile-time constants
+  float hi = 0.f, lo = 0.f, hi2 = 0.f, lo2 = 0.f;
+  if (r0 < r1) issue(r0, stage);
+  cp_async_commit();
+  int t = 0;
+  for (int64_t r = r0; r < r1; r += T, ++t) {
+    float2* cur = stage + (t & 1) * ssz;
+    if (r + T < r1) issue(r + T, stage + ((t + 1) & 1) * ssz);
+    cp_async_commit();
+    cp_async_wait1();
+    __syncthreads();
+    if (mine) {
+      const int nr = (int)min((int64_t)T, r1 - r);
+      const int share = (nr + rg - 1) / rg;
+      const int rb = rgi * share, re = min(nr, rb + share);
+      const float2* ap = cur + aoff + rb * NSD;
+      const float2* bp = cur + T * wA + j + rb * NBC;
+      int rr = rb;
+      for (; rr + 16 <= re; rr += 16, ap += 16 * NSD, bp += 16 * NBC) {
+#pragma unroll
+        for (int k = 0; k < 16; k += 2) {
+          const float2 a0 = ap[k * NSD], a1 = ap[(k + 1) * NSD];
+          const float2 b0 = bp[k * NBC], b1 = bp[(k + 1) * NBC];
+          ff_mac(hi, lo, a0.x, a0.y, b0.x, b0.y);
+          ff_mac(hi2, lo2, a1.x, a1.y, b1.x, b1.y);
+        }
+        ff_renorm(hi, lo);
+        ff_renorm(hi2, lo2);
+      }
+      for (; rr < re; ++rr, ap += NSD, bp += NBC) {
+        const float2 a0 = ap[0], b0 = bp[0];
+        ff_mac(hi, lo, a0.x, a0.y, b0.x, b0.y);
+      }
+      ff_renorm(hi, lo);
+    }
+    __syncthreads();
+  }
+  if (active) red[w][lane] = ((double)hi + (double)lo) + ((double)hi2 + (double)lo2);
+  __syncthreads();
+  if (w < ncg_here) {
+    double v = 0.0;
+    for (int g = 0; g < rg; ++g) v += red[g * ncg_here + w][lane];
+    const int i = (cg0 + w) * CI + q;
+    if (q < CI && i < m) partial[(int64_t)blockIdx.x * m * NBC + (int64_t)i * NBC + j] = v;
+  }
+}
+
 // out_t[r][0:nsd] = sum_i A_t[column i][r] C[i][0:nsd] for up to 3 (A, out)
 // pairs sharing C (m x nsd, row-major; the m columns are nb consecutive blocks
 // of nsd).  A lane owns one row: per block it loads the row's NSD values
@@ -318,7 +506,8 @@ __global__ void __launch_bounds__(DBLK) k_lincomb(LinComb L, int nb, int64_t N, 
 // FP32 sigma on most iterations.  Same row ownership, loads and summation
 // order as k_lincomb.
 template <int NSD>
-__global__ void __launch_bounds__(DBLK) k_lincomb_ff(LinComb L, int nb, int64_t N, const double* C) {
+__global__ void __launch_bounds__(DBLK) k_lincomb_ff(LinComb L, int nb, int64_t N, const double* C, const int* skip) {
+  if (skip && *skip) return;
   __shared__ float2 Cs[MAXM * MAXS];
   for (int i = threadIdx.x; i < nb * NSD * NSD; i += DBLK) {
     float h, l;
@@ -345,15 +534,7 @@ __global__ void __launch_bounds__(DBLK) k_lincomb_ff(LinComb L, int nb, int64_t 
 #pragma unroll
           for (int j = 0; j < NSD; ++j) {
             const float2 cv = cb[c * NSD + j];
-            const float p = __fmul_rn(xh, cv.x);
-            float pe = __fmaf_rn(xh, cv.x, -p);
-            pe = __fmaf_rn(xh, cv.y, pe);
-            pe = __fmaf_rn(xl, cv.x, pe);
-            const float s = __fadd_rn(ah[j], p);
-            const float bb = __fsub_rn(s, ah[j]);
-            const float err = __fadd_rn(__fsub_rn(ah[j], __fsub_rn(s, bb)), __fsub_rn(p, bb));
-            ah[j] = s;
-            al[j] = __fadd_rn(al[j], __fadd_rn(err, pe));
+            ff_mac(ah[j], al[j], xh, xl, cv.x, cv.y);
           }
         }
 #pragma unroll
@@ -366,42 +547,56 @@ __global__ void __launch_bounds__(DBLK) k_lincomb_ff(LinComb L, int nb, int64_t 
   }
 }
 
-// Cholesky G = R^T R (nsd x nsd) and Rinv = R^-1 (row-major, upper), one
-// thread.  A vanishing pivot (dependent column) gives a zero column.
+// Cholesky G = R^T R (n x n, n <= MAXS, in shared memory) and Ri = R^-1
+// (upper triangular), by one warp: row j of R is formed by lanes i >= j
+// after its pivot, and lane j back-substitutes column j of R^-1.  Every sum
+// runs in the order of the one-thread algorithm (k ascending), so the result
+// does not depend on the lane layout.  A vanishing pivot (a dependent
+// column) gives a zero row of R and a zero column of Ri.
+__device__ void chol_inv_warp(const double (*G)[MAXS], double (*R)[MAXS], double (*Ri)[MAXS], int n, int lane) {
+  for (int j = 0; j < n; ++j) {
+    double dj = G[j][j];
+    for (int k = 0; k < j; ++k) dj -= R[k][j] * R[k][j];
+    const bool ok = (dj > 1e-28 * fabs(G[j][j])) && (dj > 1e-300);
+    const double rjj = ok ? sqrt(dj) : 0.0;
+    if (lane < n) {
+      double v = 0.0;
+      if (lane == j) {
+        v = rjj;
+      } else if (lane > j && ok) {
+        double t = G[j][lane];
+        for (int k = 0; k < j; ++k) t -= R[k][j] * R[k][lane];
+        v = t / rjj;
+      }
+      R[j][lane] = v;
+    }
+    __syncwarp();
+  }
+  if (lane < n) {
+    const int j = lane;
+    for (int i = 0; i < n; ++i) Ri[i][j] = 0.0;
+    if (R[j][j] != 0.0) {
+      Ri[j][j] = 1.0 / R[j][j];
+      for (int i = j - 1; i >= 0; --i) {
+        if (R[i][i] == 0.0) continue;
+        double t = 0.0;
+        for (int k = i + 1; k <= j; ++k) t += R[i][k] * Ri[k][j];
+        Ri[i][j] = -t / R[i][i];
+      }
+    }
+  }
+  __syncwarp();
+}
+
+// Rinv = R^-1 for the Cholesky factor of G (nsd x nsd, row-major), one warp
 __global__ void k_chol_inv(const double* G, int nsd, double* Rinv) {
-  if (threadIdx.x || blockIdx.x) return;
-  double R[MAXS][MAXS], Ri[MAXS][MAXS];
-  for (int i = 0; i < nsd; ++i)
-    for (int j = 0; j < nsd; ++j) R[i][j] = Ri[i][j] = 0.0;
-  for (int j = 0; j < nsd; ++j) {
-    double d = G[j * nsd + j];
-    for (int k = 0; k < j; ++k) d -= R[k][j] * R[k][j];
-    const double scale = fabs(G[j * nsd + j]);
-    if (!(d > 1e-28 * scale) || !(d > 1e-300)) {
-      for (int k = 0; k < nsd; ++k) R[j][k] = 0.0;
-      R[j][j] = 0.0;
-      continue;
-    }
-    R[j][j] = sqrt(d);
-    for (int i = j + 1; i < nsd; ++i) {
-      double s = G[j * nsd + i];
-      for (int k = 0; k < j; ++k) s -= R[k][j] * R[k][i];
-      R[j][i] = s / R[j][j];
-    }
-  }
-  // back substitution: Ri = R^-1 (upper triangular); zero pivot -> zero column
-  for (int j = nsd - 1; j >= 0; --j) {
-    if (R[j][j] == 0.0) continue;
-    Ri[j][j] = 1.0 / R[j][j];
-    for (int i = j - 1; i >= 0; --i) {
-      if (R[i][i] == 0.0) continue;
-      double s = 0.0;
-      for (int k = i + 1; k <= j; ++k) s += R[i][k] * Ri[k][j];
-      Ri[i][j] = -s / R[i][i];
-    }
-  }
-  for (int i = 0; i < nsd; ++i)
-    for (int j = 0; j < nsd; ++j) Rinv[i * nsd + j] = Ri[i][j];
+  __shared__ double Gs[MAXS][MAXS], R[MAXS][MAXS], Ri[MAXS][MAXS];
+  const int lane = threadIdx.x & 31;
+  if (threadIdx.x >= 32) return;
+  for (int idx = lane; idx < nsd * nsd; idx += 32) Gs[idx / nsd][idx % nsd] = G[idx];
+  __syncwarp();
+  chol_inv_warp(Gs, R, Ri, nsd, lane);
+  for (int idx = lane; idx < nsd * nsd; idx += 32) Rinv[idx] = Ri[idx / nsd][idx % nsd];
 }
 
 // Coefficients of the fused classical Gram-Schmidt + Cholesky-QR update of a
@@ -417,7 +612,7 @@ __global__ void k_chol_inv(const double* G, int nsd, double* Rinv) {
 // dependent column) gives a zero column, as in k_chol_inv.
 __global__ void k_cgs_coef(const double* X, int m, int nsd, double* K, int* skip2, int mode) {
   if (mode == 1 && *skip2) return;
-  __shared__ double G[MAXS][MAXS], Ri[MAXS][MAXS];
+  __shared__ double G[MAXS][MAXS], R[MAXS][MAXS], Ri[MAXS][MAXS];
   __shared__ int need;
   for (int idx = threadIdx.x; idx < nsd * nsd; idx += blockDim.x) {
     const int i = idx / nsd, j = idx % nsd;
@@ -433,33 +628,9 @@ __global__ void k_cgs_coef(const double* X, int m, int nsd, double* K, int* skip
         if (!(G[j][j] > 0.25 * X[(m + j) * nsd + j])) nd = 1;
     need = nd;
     if (mode == 0) *skip2 = nd ? 0 : 1;
-    if (!nd) {
-      double R[MAXS][MAXS];
-      for (int i = 0; i < nsd; ++i)
-        for (int j = 0; j < nsd; ++j) R[i][j] = Ri[i][j] = 0.0;
-      for (int j = 0; j < nsd; ++j) {
-        double dj = G[j][j];
-        for (int k = 0; k < j; ++k) dj -= R[k][j] * R[k][j];
-        if (!(dj > 1e-28 * fabs(G[j][j])) || !(dj > 1e-300)) continue;  // zero row of R
-        R[j][j] = sqrt(dj);
-        for (int i = j + 1; i < nsd; ++i) {
-          double t = G[j][i];
-          for (int k = 0; k < j; ++k) t -= R[k][j] * R[k][i];
-          R[j][i] = t / R[j][j];
-        }
-      }
-      for (int j = nsd - 1; j >= 0; --j) {
-        if (R[j][j] == 0.0) continue;
-        Ri[j][j] = 1.0 / R[j][j];
-        for (int i = j - 1; i >= 0; --i) {
-          if (R[i][i] == 0.0) continue;
-          double t = 0.0;
-          for (int k = i + 1; k <= j; ++k) t += R[i][k] * Ri[k][j];
-          Ri[i][j] = -t / R[i][i];
-        }
-      }
-    }
   }
+  __syncthreads();
+  if (!need && threadIdx.x < 32) chol_inv_warp(G, R, Ri, nsd, threadIdx.x);
   __syncthreads();
   const bool fuse = !need;
   for (int idx = threadIdx.x; idx < (m + nsd) * nsd; idx += blockDim.x) {
@@ -509,6 +680,76 @@ __global__ void __launch_bounds__(DBLK) k_step(double* Un, const double* Wn, con
 #pragma unroll
   for (int k = 0; k < MAXS; ++k) {
     double s = acc[k];
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+    if (lane == 0) red[k][w] = s;
+  }
+  __syncthreads();
+  if (threadIdx.x < MAXS) {
+    double s = 0.0;
+    for (int i = 0; i < DBLK / 32; ++i) s += red[threadIdx.x][i];
+    partial[(int64_t)blockIdx.x * MAXS + threadIdx.x] = s;
+  }
+}
+
+// FP64 -> FP32 by truncation and FP32 -> FP64 exactly, with integer
+// instructions (GB300's conversions between the two formats issue at the
+// FP64 rate).  |x| below 2^-126 gives 0; beyond the float range, or Inf or
+// NaN, gives a signed Inf (so a diverging step still reads as non-finite).
+__device__ __forceinline__ float f32_trunc(double x) {
+  const unsigned long long b = (unsigned long long)__double_as_longlong(x);
+  const unsigned h32 = (unsigned)(b >> 32), l32 = (unsigned)b;
+  const unsigned sign = h32 & 0x80000000u;
+  const int fe = (int)((h32 >> 20) & 0x7ffu) - 896;
+  if (fe <= 0) return __uint_as_float(sign);
+  if (fe >= 255) return __uint_as_float(sign | 0x7f800000u);
+  return __uint_as_float(sign | ((unsigned)fe << 23) | ((h32 & 0xfffffu) << 3) | (l32 >> 29));
+}
+__device__ __forceinline__ double f64_from(float f) {
+  const unsigned u = __float_as_uint(f);
+  const unsigned e = (u >> 23) & 0xffu;
+  const unsigned long long sign = (unsigned long long)(u & 0x80000000u) << 32;
+  if (e == 0) return __longlong_as_double((long long)sign);
+  if (e == 255) return __longlong_as_double((long long)(sign | 0x7ff0000000000000ull));
+  return __longlong_as_double(
+      (long long)(sign | ((unsigned long long)(e + 896) << 52) | ((unsigned long long)(u & 0x7fffffu) << 29)));
+}
+
+// The Davidson step of k_step for the mixed-precision loop: the residual
+// numerator lambda u - W is formed by one FP64 FMA (it cancels near
+// convergence), then the S^2 factor, the diagonal preconditioner and the
+// squared norms run in FP32 -- the accuracy of the FP32 sigma that feeds
+// most of these iterations; the step is a search direction and its norm the
+// convergence measure, both needed to a few digits.
+__global__ void __launch_bounds__(DBLK) k_step_mixed(double* Un, const double* Wn, const double* Sn, const double* hjj,
+                                                     int64_t N, StepParams p, double* partial) {
+  __shared__ double red[MAXS][DBLK / 32];
+  float acc[MAXS];
+#pragma unroll
+  for (int k = 0; k < MAXS; ++k) acc[k] = 0.f;
+  const float sz2sz = (float)p.sz2sz;
+  float s2f[MAXS];
+#pragma unroll
+  for (int k = 0; k < MAXS; ++k) s2f[k] = (float)p.s2[k];
+  for (int64_t r = blockIdx.x * (int64_t)DBLK + threadIdx.x; r < N; r += (int64_t)gridDim.x * DBLK) {
+    const double h = hjj[r];
+#pragma unroll
+    for (int k = 0; k < MAXS; ++k) {
+      if (k >= p.nsd) break;
+      const int64_t x = r * p.nsd + k;
+      const double u = Un[x];
+      const float num = f32_trunc(fma(p.lambda[k], u, -Wn[x]));
+      const float fac = 1.0f + s2f[k] * f32_trunc(u) - f32_trunc(Sn[x]) - sz2sz;
+      const float den = fmaxf(f32_trunc(h - p.lambda[k]), 1e-2f);
+      const float v = __fdiv_rn(num * fac, den);
+      Un[x] = f64_from(v);
+      if (k < p.nst) acc[k] = fmaf(v, v, acc[k]);
+    }
+  }
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+#pragma unroll
+  for (int k = 0; k < MAXS; ++k) {
+    double s = (double)acc[k];
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
     if (lane == 0) red[k][w] = s;
@@ -711,6 +952,8 @@ struct Dav {
   double* small = nullptr;  // device small matrices (MAXM*MAXS x 6)
   float *cX = nullptr, *cd = nullptr, *cc = nullptr;  // training capture
   float *mlpX = nullptr, *mlpG = nullptr;              // learned step: features, multipliers
+  float2 *Uf = nullptr, *Bf = nullptr;  // mixed precision: split U blocks, split [W_b S_b]
+  int64_t sUf = 0;                       // block stride of Uf (float2)
   int ncta = 0;
   int64_t rows_per_cta = 0;
   ~Dav() {
@@ -726,6 +969,8 @@ struct Dav {
     dev_free(cc);
     dev_free(mlpX);
     dev_free(mlpG);
+    dev_free(Uf);
+    dev_free(Bf);
   }
   double* blk(double* X, int b) const { return X + (int64_t)b * N * nsd; }
 };
@@ -746,8 +991,8 @@ int gram(Dav& d, const double* A, int m, const double* B0, const double* B1, dou
   const int ncg = (m + ci - 1) / ci;
   const dim3 grid(d.ncta, (ncg + DBLK / 32 - 1) / (DBLK / 32));
   const int64_t sA = d.N * d.nsd;
-#define QP_GRAM_CASE(NB)                                                                                      \
-  case NB:                                                                                                    \
+#define QP_GRAM_CASE(NB)                                                                      \
+  case NB:                                                                                    \
     k_gram<NB><<<grid, DBLK, 0, d.st>>>(A, m, sA, B0, B1, d.nsd, d.N, d.rows_per_cta, d.part, skip); \
     break;
   switch (nbc) {
@@ -767,6 +1012,62 @@ int gram(Dav& d, const double* A, int m, const double* B0, const double* B1, dou
       return -1;
   }
 #undef QP_GRAM_CASE
+  k_reduce_partials<<<gsz((int64_t)m * nbc * 32), DBLK, 0, d.st>>>(d.part, d.ncta, m * nbc, out, skip);
+  return 0;
+}
+
+// float-float copy of one block (X1 = nullptr) or of [X0 X1]
+void split_block(Dav& d, const double* X0, const double* X1, float2* out, const int* skip = nullptr) {
+  const int nx = X1 ? 2 : 1;
+  k_split_block<<<std::min<unsigned>(gsz(d.N * d.nsd), 152 * 8), DBLK, 0, d.st>>>(X0, X1, d.nsd, nx, d.N, out, skip);
+}
+
+// out (m x nbc) = A^T B on split operands: A = m columns of consecutive split
+// blocks, B = rows of nbc split values
+int gram_ff(Dav& d, const float2* A, int m, const float2* B, int nbc, double* out, const int* skip = nullptr) {
+  const int ci = 32 / nbc;
+  const int ncg = (m + ci - 1) / ci;
+  const dim3 grid(d.ncta, (ncg + DBLK / 32 - 1) / (DBLK / 32));
+  const int width = gram_stage_width(m, d.nsd, nbc);
+  const int T = gram_rows_per_stage(width);
+  const size_t smem = (size_t)2 * T * width * sizeof(float2);
+  static int smem_set[2][MAXS + 1] = {};  // dynamic shared memory opted in per instantiation
+  const bool two = nbc == 2 * d.nsd;
+  if (!two && nbc != d.nsd) return -1;
+#define QP_GRAMF_CASE(NS)                                                                               \
+  case NS:                                                                                              \
+    if (two) {                                                                                          \
+      if ((int)smem > smem_set[1][NS]) {                                                                \
+        cudaFuncSetAttribute(k_gram_ff<2 * NS, NS>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem); \
+        cudaFuncSetAttribute(k_gram_ff<2 * NS, NS>, cudaFuncAttributePreferredSharedMemoryCarveout,      \
+                             cudaSharedmemCarveoutMaxShared);                                           \
+        smem_set[1][NS] = (int)smem;                                                                    \
+      }                                                                                                 \
+      k_gram_ff<2 * NS, NS><<<grid, DBLK, smem, d.st>>>(A, m, d.sUf, B, d.N, d.rows_per_cta, T, d.part, skip); \
+    } else {                                                                                            \
+      if ((int)smem > smem_set[0][NS]) {                                                                \
+        cudaFuncSetAttribute(k_gram_ff<NS, NS>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);  \
+        cudaFuncSetAttribute(k_gram_ff<NS, NS>, cudaFuncAttributePreferredSharedMemoryCarveout,          \
+                             cudaSharedmemCarveoutMaxShared);                                           \
+        smem_set[0][NS] = (int)smem;                                                                    \
+      }                                                                                                 \
+      k_gram_ff<NS, NS><<<grid, DBLK, smem, d.st>>>(A, m, d.sUf, B, d.N, d.rows_per_cta, T, d.part, skip); \
+    }                                                                                                   \
+    break;
+  // the 48 KB default counts the static red[] too, so every size is opted in
+  switch (d.nsd) {
+    QP_GRAMF_CASE(1)
+    QP_GRAMF_CASE(2)
+    QP_GRAMF_CASE(3)
+    QP_GRAMF_CASE(4)
+    QP_GRAMF_CASE(5)
+    QP_GRAMF_CASE(6)
+    QP_GRAMF_CASE(7)
+    QP_GRAMF_CASE(8)
+    default:
+      return -1;
+  }
+#undef QP_GRAMF_CASE
   k_reduce_partials<<<gsz((int64_t)m * nbc * 32), DBLK, 0, d.st>>>(d.part, d.ncta, m * nbc, out, skip);
   return 0;
 }
@@ -806,24 +1107,30 @@ void lincomb(Dav& d, int m, const double* C, const double* A0, double* O0, const
   }
 }
 
-// the same linear combination of three (A, out) pairs in float-float
-// arithmetic (mixed-precision Ritz vectors)
-void lincomb_ff(Dav& d, int m, const double* C, const double* A0, double* O0, const double* A1, double* O1,
-                const double* A2, double* O2) {
+// the same linear combination in float-float arithmetic (mixed precision:
+// Ritz vectors, Gram-Schmidt updates, re-contraction)
+void lincomb_ff(Dav& d, int m, const double* C, const double* A0, double* O0, const double* A1 = nullptr,
+                double* O1 = nullptr, const double* A2 = nullptr, double* O2 = nullptr, const int* skip = nullptr) {
   LinComb L{};
   L.A[0] = A0;
   L.out[0] = O0;
-  L.A[1] = A1;
-  L.out[1] = O1;
-  L.A[2] = A2;
-  L.out[2] = O2;
-  L.n = 3;
+  L.n = 1;
+  if (A1) {
+    L.A[1] = A1;
+    L.out[1] = O1;
+    L.n = 2;
+  }
+  if (A2) {
+    L.A[2] = A2;
+    L.out[2] = O2;
+    L.n = 3;
+  }
   const int nb = m / d.nsd;
   const unsigned grid = std::min<unsigned>(gsz(d.N), 152 * 8);
   switch (d.nsd) {
 #define QP_LCF_CASE(NS) \
   case NS:              \
-    k_lincomb_ff<NS><<<grid, DBLK, 0, d.st>>>(L, nb, d.N, C); \
+    k_lincomb_ff<NS><<<grid, DBLK, 0, d.st>>>(L, nb, d.N, C, skip); \
     break;
     QP_LCF_CASE(1)
     QP_LCF_CASE(2)
@@ -840,8 +1147,9 @@ void lincomb_ff(Dav& d, int m, const double* C, const double* A0, double* O0, co
 // orthonormalise block b against blocks 0..b-1 and within itself: one fused
 // Gram-Schmidt + Cholesky-QR pass (k_cgs_coef), a second one when the first
 // lost more than half of a column's norm, then a Cholesky-QR pass on the
-// block alone (CholQR2)
-void orthonormalise(Dav& d, int b) {
+// block alone (CholQR2).  ff = true: Gram blocks and updates in float-float
+// (the small factorisations stay FP64)
+void orthonormalise(Dav& d, int b, bool ff) {
   double* Ub = d.blk(d.U, b);
   double* X = d.small + OFF_X;
   double* K = d.small + OFF_K;
@@ -849,19 +1157,42 @@ void orthonormalise(Dav& d, int b) {
   double* Rinv = d.small + OFF_RINV;
   int* skip2 = (int*)(d.small + OFF_FLAG);
   const int m = b * d.nsd, m1 = m + d.nsd;
+  if (!ff) {
+    if (b > 0) {
+      gram(d, d.U, m1, Ub, nullptr, X);
+      k_cgs_coef<<<1, 128, 0, d.st>>>(X, m, d.nsd, K, skip2, 0);
+      lincomb(d, m1, K, d.U, Ub);
+      gram(d, d.U, m1, Ub, nullptr, X, skip2);
+      k_cgs_coef<<<1, 128, 0, d.st>>>(X, m, d.nsd, K, skip2, 1);
+      lincomb(d, m1, K, d.U, Ub, nullptr, nullptr, nullptr, nullptr, skip2);
+    }
+    for (int pass = (b > 0) ? 1 : 0; pass < 2; ++pass) {
+      gram(d, Ub, d.nsd, Ub, nullptr, G);
+      k_chol_inv<<<1, 32, 0, d.st>>>(G, d.nsd, Rinv);
+      lincomb(d, d.nsd, Rinv, Ub, Ub);
+    }
+    return;
+  }
+  // float-float: the Gram blocks read the split copies Uf (blocks 0..b-1 are
+  // split when they are finished; block b is split before each use)
+  float2* Ufb = d.Uf + (int64_t)b * d.sUf;
   if (b > 0) {
-    gram(d, d.U, m1, Ub, nullptr, X);
+    split_block(d, Ub, nullptr, Ufb);
+    gram_ff(d, d.Uf, m1, Ufb, d.nsd, X);
     k_cgs_coef<<<1, 128, 0, d.st>>>(X, m, d.nsd, K, skip2, 0);
-    lincomb(d, m1, K, d.U, Ub);
-    gram(d, d.U, m1, Ub, nullptr, X, skip2);
+    lincomb_ff(d, m1, K, d.U, Ub);
+    split_block(d, Ub, nullptr, Ufb, skip2);
+    gram_ff(d, d.Uf, m1, Ufb, d.nsd, X, skip2);
     k_cgs_coef<<<1, 128, 0, d.st>>>(X, m, d.nsd, K, skip2, 1);
-    lincomb(d, m1, K, d.U, Ub, nullptr, nullptr, nullptr, nullptr, skip2);
+    lincomb_ff(d, m1, K, d.U, Ub, nullptr, nullptr, nullptr, nullptr, skip2);
   }
   for (int pass = (b > 0) ? 1 : 0; pass < 2; ++pass) {
-    gram(d, Ub, d.nsd, Ub, nullptr, G);
-    k_chol_inv<<<1, 1, 0, d.st>>>(G, d.nsd, Rinv);
-    lincomb(d, d.nsd, Rinv, Ub, Ub);
+    split_block(d, Ub, nullptr, Ufb);
+    gram_ff(d, Ufb, d.nsd, Ufb, d.nsd, G);
+    k_chol_inv<<<1, 32, 0, d.st>>>(G, d.nsd, Rinv);
+    lincomb_ff(d, d.nsd, Rinv, Ub, Ub);
   }
+  split_block(d, Ub, nullptr, Ufb);
 }
 
 // Per-phase stream timeline of one Davidson run (environment QPGPU_PROFILE=1):
@@ -940,6 +1271,11 @@ extern "C" int qpgpu_davidson_hs2(qpgpu_ctx* c, double* u_in, int64_t dim_in, do
     cudaGetLastError();
     return qpgpu_fail(c, QPGPU_ERR_NOMEM, "Davidson work arrays do not fit on the device");
   }
+  d.sUf = (int64_t)blkn;
+  if (mixed && (dev_alloc(&d.Uf, blkn * itermax) != cudaSuccess || dev_alloc(&d.Bf, blkn * 2) != cudaSuccess)) {
+    cudaGetLastError();
+    return qpgpu_fail(c, QPGPU_ERR_NOMEM, "mixed-precision work arrays do not fit on the device");
+  }
   cudaStream_t st = d.st;
   // learned preconditioner and training capture
   const bool use_mlp = prm->preconditioner == 1 || prm->preconditioner == 2;
@@ -1016,7 +1352,7 @@ extern "C" int qpgpu_davidson_hs2(qpgpu_ctx* c, double* u_in, int64_t dim_in, do
       const int b = iter - 1;
       const int shift = nsd * b;
       shift2 = nsd * iter;
-      orthonormalise(d, b);
+      orthonormalise(d, b, mixed);
       prof.mark(DavProf::ORTHO);
       // sigma on block b
       const int prec = (mixed && iter > 1) ? QPGPU_FP32 : restart_prec;
@@ -1030,7 +1366,12 @@ extern "C" int qpgpu_davidson_hs2(qpgpu_ctx* c, double* u_in, int64_t dim_in, do
       prof.mark(DavProf::SIGMA);
       // new Gram columns
       // h(:, new) and s(:, new) in one pass over U: X = U^T [W_b S_b]
-      gram(d, d.U, shift2, d.blk(d.W, b), d.blk(d.S, b), d.small + OFF_X);
+      if (mixed) {
+        split_block(d, d.blk(d.W, b), d.blk(d.S, b), d.Bf);
+        gram_ff(d, d.Uf, shift2, d.Bf, 2 * nsd, d.small + OFF_X);
+      } else {
+        gram(d, d.U, shift2, d.blk(d.W, b), d.blk(d.S, b), d.small + OFF_X);
+      }
       QP_CUDA(c, cudaMemcpyAsync(hscol.data(), d.small + OFF_X, (size_t)shift2 * 2 * nsd * sizeof(double),
                                  cudaMemcpyDeviceToHost, st));
       QP_CUDA(c, cudaStreamSynchronize(st));
@@ -1089,7 +1430,7 @@ extern "C" int qpgpu_davidson_hs2(qpgpu_ctx* c, double* u_in, int64_t dim_in, do
       double* ydev = d.small + OFF_Y;
       prof.mark(DavProf::HOST);
       QP_CUDA(c, cudaMemcpyAsync(ydev, ycoef.data(), ycoef.size() * sizeof(double), cudaMemcpyHostToDevice, st));
-      if (mixed)  // Ritz vectors in float-float (the FP64 list is projection, eigensolve, GS, norms)
+      if (mixed)  // Ritz vectors in float-float (FP64: the small eigenproblem, factorisations, step, norms)
         lincomb_ff(d, shift2, ydev, d.U, d.blk(d.U, iter), d.W, d.blk(d.W, iter), d.S, d.blk(d.S, iter));
       else
         lincomb(d, shift2, ydev, d.U, d.blk(d.U, iter), d.W, d.blk(d.W, iter), d.S, d.blk(d.S, iter));
@@ -1119,6 +1460,9 @@ extern "C" int qpgpu_davidson_hs2(qpgpu_ctx* c, double* u_in, int64_t dim_in, do
         k_step_mlp<<<d.ncta, DBLK, 0, st>>>(d.blk(d.U, iter), d.blk(d.W, iter), d.blk(d.S, iter), c->d_hdiag, d.mlpG,
                                             N, sp, mask, mlp_extra, d.part);
       }
+      else if (mixed)
+        k_step_mixed<<<d.ncta, DBLK, 0, st>>>(d.blk(d.U, iter), d.blk(d.W, iter), d.blk(d.S, iter), c->d_hdiag, N, sp,
+                                              d.part);
       else
         k_step<<<d.ncta, DBLK, 0, st>>>(d.blk(d.U, iter), d.blk(d.W, iter), d.blk(d.S, iter), c->d_hdiag, N, sp, d.part);
       QP_CUDA(c, cudaGetLastError());
@@ -1168,7 +1512,10 @@ extern "C" int qpgpu_davidson_hs2(qpgpu_ctx* c, double* u_in, int64_t dim_in, do
       for (int j = 0; j < nsd; ++j) ycoef[(size_t)i * nsd + j] = y[(size_t)i * shift2 + j];
     double* ydev = d.small + OFF_Y;
     QP_CUDA(c, cudaMemcpyAsync(ydev, ycoef.data(), ycoef.size() * sizeof(double), cudaMemcpyHostToDevice, st));
-    lincomb(d, shift2, ydev, d.U, d.R);
+    if (mixed)
+      lincomb_ff(d, shift2, ydev, d.U, d.R);
+    else
+      lincomb(d, shift2, ydev, d.U, d.R);
     k_copy<<<gsz((int64_t)blkn), DBLK, 0, st>>>(d.R, d.U, (int64_t)blkn);
     prof.mark(DavProf::RESTART);
     for (int i = 0; i < mmax; ++i)

@@ -3,7 +3,8 @@ davidson_diag_hjj_sjj and against dense eigen-solves of golden matrices.
 
 Bars: FP64 eigenvalues within 1e-9 Ha of the oracle / of the dense
 eigenvalues; mixed precision (FP32 sigma, FP64 sigma at each restart) within
-1e-6 Ha of the FP64 device run.  The seeded selected spaces are not spin
+1e-6 Ha of the FP64 device run at threshold 1e-10 and within 1e-9 Ha at
+1e-12 (both restart sigmas).  The seeded selected spaces are not spin
 complete, so their runs use s2_eig = False (lowest eigenvalues of H in the
 space); the full-CI golden spaces keep s2_eig = True.  Every run is capped.
 """
@@ -67,18 +68,21 @@ def test_davidson_mixed_precision_within_1e6():
     assert (tr["precision"] == FP32).any() and tr["precision"][-1] == FP64
 
 
-def test_davidson_float_float_restart_sigma():
-    # QPGPU_FF: FP32 sigma with the float-float sigma as the restart sigma;
+@pytest.mark.parametrize("prec_name,nsd,nst", [("FF", 8, 4), ("FP32", 8, 4), ("FP32", 3, 2)])
+def test_davidson_mixed_tight(prec_name, nsd, nst):
+    # both mixed modes (FP32 sigma, the FP64 or float-float sigma at each
+    # restart; float-float Gram-Schmidt, projections and Ritz vectors):
     # converged eigenvalues as accurate as the FP64 loop's
     from quantum_package_gb300 import FF
     from quantum_package_gb300.sigma import Wavefunction
+    prec = {"FF": FF, "FP32": FP32}[prec_name]
     p = G.make_problem(2, n_det=20_000, n_states=4)
     wf = Wavefunction.from_problem(p)
-    u = _guess(p.n_det, 8, 3)
-    kw = dict(n_states=4, threshold=1e-12, s2_eig=False, max_iter=500)
+    u = _guess(p.n_det, nsd, 3)
+    kw = dict(n_states=nst, threshold=1e-12, s2_eig=False, max_iter=500)
     r64 = wf.davidson_diag_hs2(u, **kw)
-    rff = wf.davidson_diag_hs2(u, precision=FF, **kw)
-    assert r64["converged"] and rff["converged"]
-    np.testing.assert_allclose(rff["energies"][:4], r64["energies"][:4], rtol=0, atol=1e-9)
-    tr = rff["trace"]
-    assert (tr["precision"] == FP32).any() and tr["precision"][-1] == FF
+    rm = wf.davidson_diag_hs2(u, precision=prec, **kw)
+    assert r64["converged"] and rm["converged"]
+    np.testing.assert_allclose(rm["energies"][:nst], r64["energies"][:nst], rtol=0, atol=1e-9)
+    tr = rm["trace"]
+    assert (tr["precision"] == FP32).any() and tr["precision"][-1] == (FF if prec == FF else FP64)
