@@ -547,6 +547,45 @@ __global__ void __launch_bounds__(DBLK) k_lincomb_ff(LinComb L, int nb, int64_t 
   }
 }
 
+// k_lincomb in FP32 arithmetic (inputs truncated to FP32, outputs widened
+// exactly): the Ritz vectors U y, W y, S y of the mixed-precision Davidson on
+// the iterations whose W and S come from the FP32 sigma, where they only
+// feed the step; restart iterations and the re-contraction use k_lincomb_ff.
+__device__ __forceinline__ float f32_trunc(double x);
+__device__ __forceinline__ double f64_from(float f);
+template <int NSD>
+__global__ void __launch_bounds__(DBLK) k_lincomb32(LinComb L, int nb, int64_t N, const double* C) {
+  __shared__ float Cs[MAXM * MAXS];
+  for (int i = threadIdx.x; i < nb * NSD * NSD; i += DBLK) Cs[i] = f32_trunc(C[i]);
+  __syncthreads();
+  const int64_t sA = N * NSD;
+  for (int64_t r = blockIdx.x * (int64_t)DBLK + threadIdx.x; r < N; r += (int64_t)gridDim.x * DBLK) {
+    for (int t = 0; t < L.n; ++t) {
+      const double* a = L.A[t] + r * NSD;
+      float acc[NSD];
+      double x[NSD], xn[NSD];
+#pragma unroll
+      for (int j = 0; j < NSD; ++j) acc[j] = 0.f;
+      load_row<NSD>(a, x);
+      for (int b = 0; b < nb; ++b) {
+        if (b + 1 < nb) load_row<NSD>(a + (int64_t)(b + 1) * sA, xn);
+        const float* cb = Cs + b * NSD * NSD;
+#pragma unroll
+        for (int c = 0; c < NSD; ++c) {
+          const float xc = f32_trunc(x[c]);
+#pragma unroll
+          for (int j = 0; j < NSD; ++j) acc[j] = fmaf(xc, cb[c * NSD + j], acc[j]);
+        }
+#pragma unroll
+        for (int c = 0; c < NSD; ++c) x[c] = xn[c];
+      }
+      double* o = L.out[t] + r * NSD;
+#pragma unroll
+      for (int j = 0; j < NSD; ++j) o[j] = f64_from(acc[j]);
+    }
+  }
+}
+
 // Cholesky G = R^T R (n x n, n <= MAXS, in shared memory) and Ri = R^-1
 // (upper triangular), by one warp: row j of R is formed by lanes i >= j
 // after its pivot, and lane j back-substitutes column j of R^-1.  Every sum
@@ -1144,6 +1183,36 @@ void lincomb_ff(Dav& d, int m, const double* C, const double* A0, double* O0, co
   }
 }
 
+// the Ritz-vector combination of three (A, out) pairs in FP32 (k_lincomb32)
+void lincomb32(Dav& d, int m, const double* C, const double* A0, double* O0, const double* A1, double* O1,
+               const double* A2, double* O2) {
+  LinComb L{};
+  L.A[0] = A0;
+  L.out[0] = O0;
+  L.A[1] = A1;
+  L.out[1] = O1;
+  L.A[2] = A2;
+  L.out[2] = O2;
+  L.n = 3;
+  const int nb = m / d.nsd;
+  const unsigned grid = std::min<unsigned>(gsz(d.N), 152 * 8);
+  switch (d.nsd) {
+#define QP_LC32_CASE(NS) \
+  case NS:               \
+    k_lincomb32<NS><<<grid, DBLK, 0, d.st>>>(L, nb, d.N, C); \
+    break;
+    QP_LC32_CASE(1)
+    QP_LC32_CASE(2)
+    QP_LC32_CASE(3)
+    QP_LC32_CASE(4)
+    QP_LC32_CASE(5)
+    QP_LC32_CASE(6)
+    QP_LC32_CASE(7)
+    QP_LC32_CASE(8)
+#undef QP_LC32_CASE
+  }
+}
+
 // orthonormalise block b against blocks 0..b-1 and within itself: one fused
 // Gram-Schmidt + Cholesky-QR pass (k_cgs_coef), a second one when the first
 // lost more than half of a column's norm, then a Cholesky-QR pass on the
@@ -1430,7 +1499,9 @@ extern "C" int qpgpu_davidson_hs2(qpgpu_ctx* c, double* u_in, int64_t dim_in, do
       double* ydev = d.small + OFF_Y;
       prof.mark(DavProf::HOST);
       QP_CUDA(c, cudaMemcpyAsync(ydev, ycoef.data(), ycoef.size() * sizeof(double), cudaMemcpyHostToDevice, st));
-      if (mixed)  // Ritz vectors in float-float (FP64: the small eigenproblem, factorisations, step, norms)
+      if (prec == QPGPU_FP32)  // W, S from the FP32 sigma: Ritz vectors in FP32, they only feed the step
+        lincomb32(d, shift2, ydev, d.U, d.blk(d.U, iter), d.W, d.blk(d.W, iter), d.S, d.blk(d.S, iter));
+      else if (mixed)  // restart iteration: float-float
         lincomb_ff(d, shift2, ydev, d.U, d.blk(d.U, iter), d.W, d.blk(d.W, iter), d.S, d.blk(d.S, iter));
       else
         lincomb(d, shift2, ydev, d.U, d.blk(d.U, iter), d.W, d.blk(d.W, iter), d.S, d.blk(d.S, iter));
