@@ -284,10 +284,10 @@ def davidson_block(prob, wf):
     run("plain_fp64_learned", preconditioner=1)
     run("mixed_learned", precision=FP32, preconditioner=1)
     run("mixed_learned_extra", precision=FP32, preconditioner=2)
-    a, b = out["plain_fp64"]["time_to_E_s"], out["mixed"]["time_to_E_s"]
-    out["speedup_mixed_vs_plain"] = (a / b) if (a and b) else None
-    a, b = out["plain_fp64"]["time_to_E_s"], out["mixed_learned"]["time_to_E_s"]
-    out["speedup_mixed_learned_vs_plain"] = (a / b) if (a and b) else None
+    run("mixed_ff_restart_learned_extra", precision=FF, preconditioner=2)
+    for arm in ("mixed", "mixed_ff_restart", "mixed_learned", "mixed_learned_extra", "mixed_ff_restart_learned_extra"):
+        a, b = out["plain_fp64"]["time_to_E_s"], out[arm]["time_to_E_s"]
+        out[f"speedup_{arm}_vs_plain"] = (a / b) if (a and b) else None
     return out
 
 

@@ -1,0 +1,85 @@
+"""The 2e7-determinant configuration (16 alpha + 16 beta electrons in 120 MOs,
+N_int = 2, 2 states) on one GPU, end to end.  Opt-in (QPGPU_LARGE=1): the
+seeded set takes about 4 minutes to generate on the host, the set-up about a
+minute and each sigma about 70 s, since its 6.4e10 connected pairs do not fit
+in device memory and every sigma enumerates them (direct sigma).
+
+Checks: the direct mode is chosen by itself; sigma and S^2 sigma are
+Hermitian (u0.Hu1 = u1.Hu0 to 1e-12 relative); 21 rows spread over the set
+match the CPU oracle's rows to 1e-12 relative; and five iterations of the
+device Davidson lower both Ritz values monotonically and bring the lowest
+state's squared residual norm (the reference's measure,
+diagonalization_hs2.irp.f:395) below 1e-3 from 4e5.  Run with -s to see the
+timings it prints.
+"""
+import json
+import os
+import time
+
+import numpy as np
+import pytest
+
+from quantum_package_gb300 import generate as G
+
+pytestmark = [pytest.mark.gpu,
+              pytest.mark.skipif(os.environ.get("QPGPU_LARGE") != "1",
+                                 reason="2e7-determinant run: set QPGPU_LARGE=1")]
+
+ROW_STEP = 997_331
+
+
+@pytest.fixture(scope="module")
+def large():
+    from quantum_package_gb300.sigma import Wavefunction
+    t = time.time()
+    prob = G.make_problem(5)
+    gen_s = time.time() - t
+    t = time.time()
+    wf = Wavefunction.from_problem(prob)
+    info = wf.info()
+    print(json.dumps({"generate_s": gen_s, "set_dets_wall_s": time.time() - t,
+                      **{k: info[k] for k in ("n_det", "n_pairs", "direct_sigma", "setup_ms")}}), flush=True)
+    return prob, wf
+
+
+def test_large_direct_sigma_hermitian_and_oracle_rows(large):
+    from oracle import Oracle
+    prob, wf = large
+    assert wf.info()["direct_sigma"] == 1
+    u = G.random_coefficients(prob.n_det, 2, prob.seed)
+    t = time.time()
+    v, s = wf.H_S2_u_0_nstates_openmp(u)
+    sigma_s = time.time() - t
+    a, b = float(u[0] @ v[1]), float(u[1] @ v[0])
+    herm = abs(a - b) / max(abs(a), abs(b))
+    sa, sb = float(u[0] @ s[1]), float(u[1] @ s[0])
+    herm_s2 = abs(sa - sb) / max(abs(sa), abs(sb), 1e-300)
+    o = Oracle.from_problem(prob)
+    order = np.asarray(o.bilinear()["order"]) - 1  # 1-based psi_det indices
+    u_t = np.ascontiguousarray(u[:, order].T)
+    vo, so = o.h_s2_u0_work(u_t, 1, prob.n_det, 0, ROW_STEP)
+    rows = np.arange(0, prob.n_det, ROW_STEP)
+    dr = order[rows]
+    rel_v = float(np.abs(vo[rows] - v[:, dr].T).max() / np.abs(v[:, dr]).max())
+    rel_s = float(np.abs(so[rows] - s[:, dr].T).max() / max(np.abs(s[:, dr]).max(), 1e-300))
+    print(json.dumps({"sigma_wall_s": sigma_s, "hermiticity_rel": herm, "s2_hermiticity_rel": herm_s2,
+                      "oracle_rows": len(rows), "oracle_rel_v": rel_v, "oracle_rel_s": rel_s}), flush=True)
+    assert herm < 1e-12 and herm_s2 < 1e-12
+    assert rel_v < 1e-12 and rel_s < 1e-12
+
+
+def test_large_davidson_iterations(large):
+    prob, wf = large
+    rng = np.random.default_rng(prob.seed)
+    u = rng.normal(size=(4, prob.n_det))
+    u[0] = 0.0
+    u[0, 0] = 1.0
+    t = time.time()
+    r = wf.davidson_diag_hs2(u, n_states=2, threshold=1e-10, s2_eig=False, max_iter=5)
+    tr = r["trace"]
+    e, res = tr["energies"], tr["residuals"]
+    print(json.dumps({"wall_s": time.time() - t, "n_sigma": r["n_sigma"], "energies": e.tolist(),
+                      "residuals": res.tolist(), "elapsed_ms": tr["elapsed_ms"].tolist()}), flush=True)
+    assert r["n_sigma"] == 5 and len(e) == 5
+    assert np.all(np.diff(e, axis=0) <= 1e-9)  # Ritz values decrease (no restart within 5 iterations)
+    assert res[0, 0] > 1e3 and res[-1, 0] < 1e-3
