@@ -547,12 +547,33 @@ __global__ void __launch_bounds__(DBLK) k_lincomb_ff(LinComb L, int nb, int64_t 
   }
 }
 
+// FP64 -> FP32 by truncation and FP32 -> FP64 exactly, with integer
+// instructions (GB300's conversions between the two formats issue at the
+// FP64 rate).  |x| below 2^-126 gives 0; beyond the float range, or Inf or
+// NaN, gives a signed Inf (so a diverging step still reads as non-finite).
+__device__ __forceinline__ float f32_trunc(double x) {
+  const unsigned long long b = (unsigned long long)__double_as_longlong(x);
+  const unsigned h32 = (unsigned)(b >> 32), l32 = (unsigned)b;
+  const unsigned sign = h32 & 0x80000000u;
+  const int fe = (int)((h32 >> 20) & 0x7ffu) - 896;
+  if (fe <= 0) return __uint_as_float(sign);
+  if (fe >= 255) return __uint_as_float(sign | 0x7f800000u);
+  return __uint_as_float(sign | ((unsigned)fe << 23) | ((h32 & 0xfffffu) << 3) | (l32 >> 29));
+}
+__device__ __forceinline__ double f64_from(float f) {
+  const unsigned u = __float_as_uint(f);
+  const unsigned e = (u >> 23) & 0xffu;
+  const unsigned long long sign = (unsigned long long)(u & 0x80000000u) << 32;
+  if (e == 0) return __longlong_as_double((long long)sign);
+  if (e == 255) return __longlong_as_double((long long)(sign | 0x7ff0000000000000ull));
+  return __longlong_as_double(
+      (long long)(sign | ((unsigned long long)(e + 896) << 52) | ((unsigned long long)(u & 0x7fffffu) << 29)));
+}
+
 // k_lincomb in FP32 arithmetic (inputs truncated to FP32, outputs widened
 // exactly): the Ritz vectors U y, W y, S y of the mixed-precision Davidson on
 // the iterations whose W and S come from the FP32 sigma, where they only
 // feed the step; restart iterations and the re-contraction use k_lincomb_ff.
-__device__ __forceinline__ float f32_trunc(double x);
-__device__ __forceinline__ double f64_from(float f);
 template <int NSD>
 __global__ void __launch_bounds__(DBLK) k_lincomb32(LinComb L, int nb, int64_t N, const double* C) {
   __shared__ float Cs[MAXM * MAXS];
@@ -729,29 +750,6 @@ __global__ void __launch_bounds__(DBLK) k_step(double* Un, const double* Wn, con
     for (int i = 0; i < DBLK / 32; ++i) s += red[threadIdx.x][i];
     partial[(int64_t)blockIdx.x * MAXS + threadIdx.x] = s;
   }
-}
-
-// FP64 -> FP32 by truncation and FP32 -> FP64 exactly, with integer
-// instructions (GB300's conversions between the two formats issue at the
-// FP64 rate).  |x| below 2^-126 gives 0; beyond the float range, or Inf or
-// NaN, gives a signed Inf (so a diverging step still reads as non-finite).
-__device__ __forceinline__ float f32_trunc(double x) {
-  const unsigned long long b = (unsigned long long)__double_as_longlong(x);
-  const unsigned h32 = (unsigned)(b >> 32), l32 = (unsigned)b;
-  const unsigned sign = h32 & 0x80000000u;
-  const int fe = (int)((h32 >> 20) & 0x7ffu) - 896;
-  if (fe <= 0) return __uint_as_float(sign);
-  if (fe >= 255) return __uint_as_float(sign | 0x7f800000u);
-  return __uint_as_float(sign | ((unsigned)fe << 23) | ((h32 & 0xfffffu) << 3) | (l32 >> 29));
-}
-__device__ __forceinline__ double f64_from(float f) {
-  const unsigned u = __float_as_uint(f);
-  const unsigned e = (u >> 23) & 0xffu;
-  const unsigned long long sign = (unsigned long long)(u & 0x80000000u) << 32;
-  if (e == 0) return __longlong_as_double((long long)sign);
-  if (e == 255) return __longlong_as_double((long long)(sign | 0x7ff0000000000000ull));
-  return __longlong_as_double(
-      (long long)(sign | ((unsigned long long)(e + 896) << 52) | ((unsigned long long)(u & 0x7fffffu) << 29)));
 }
 
 // The Davidson step of k_step for the mixed-precision loop: the residual
