@@ -68,7 +68,8 @@ def test_davidson_mixed_precision_within_1e6():
     assert (tr["precision"] == FP32).any() and tr["precision"][-1] == FP64
 
 
-@pytest.mark.parametrize("prec_name,nsd,nst", [("FF", 8, 4), ("FP32", 8, 4), ("FP32", 3, 2)])
+@pytest.mark.parametrize("prec_name,nsd,nst", [("FF", 8, 4), ("FP32", 8, 4), ("FP32", 3, 2), ("FP32", 1, 1),
+                                               ("FF", 2, 2), ("FP32", 5, 3)])
 def test_davidson_mixed_tight(prec_name, nsd, nst):
     # both mixed modes (FP32 sigma, the FP64 or float-float sigma at each
     # restart; float-float Gram-Schmidt, projections and Ritz vectors):
