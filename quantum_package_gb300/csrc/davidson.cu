@@ -1068,30 +1068,23 @@ int gram_ff(Dav& d, const float2* A, int m, const float2* B, int nbc, double* ou
   const int width = gram_stage_width(m, d.nsd, nbc);
   const int T = gram_rows_per_stage(width);
   const size_t smem = (size_t)2 * T * width * sizeof(float2);
-  static int smem_set[2][MAXS + 1] = {};  // dynamic shared memory opted in per instantiation
   const bool two = nbc == 2 * d.nsd;
   if (!two && nbc != d.nsd) return -1;
-#define QP_GRAMF_CASE(NS)                                                                               \
-  case NS:                                                                                              \
-    if (two) {                                                                                          \
-      if ((int)smem > smem_set[1][NS]) {                                                                \
-        cudaFuncSetAttribute(k_gram_ff<2 * NS, NS>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem); \
-        cudaFuncSetAttribute(k_gram_ff<2 * NS, NS>, cudaFuncAttributePreferredSharedMemoryCarveout,      \
-                             cudaSharedmemCarveoutMaxShared);                                           \
-        smem_set[1][NS] = (int)smem;                                                                    \
-      }                                                                                                 \
-      k_gram_ff<2 * NS, NS><<<grid, DBLK, smem, d.st>>>(A, m, d.sUf, B, d.N, d.rows_per_cta, T, d.part, skip); \
-    } else {                                                                                            \
-      if ((int)smem > smem_set[0][NS]) {                                                                \
-        cudaFuncSetAttribute(k_gram_ff<NS, NS>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);  \
-        cudaFuncSetAttribute(k_gram_ff<NS, NS>, cudaFuncAttributePreferredSharedMemoryCarveout,          \
-                             cudaSharedmemCarveoutMaxShared);                                           \
-        smem_set[0][NS] = (int)smem;                                                                    \
-      }                                                                                                 \
-      k_gram_ff<NS, NS><<<grid, DBLK, smem, d.st>>>(A, m, d.sUf, B, d.N, d.rows_per_cta, T, d.part, skip); \
-    }                                                                                                   \
+  // opted in at every launch (the attribute belongs to the current device),
+  // and for every size: the 48 KB default counts the static red[] too
+#define QP_GRAMF_LAUNCH(NB, NS)                                                                        \
+  cudaFuncSetAttribute(k_gram_ff<NB, NS>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);     \
+  cudaFuncSetAttribute(k_gram_ff<NB, NS>, cudaFuncAttributePreferredSharedMemoryCarveout,              \
+                       cudaSharedmemCarveoutMaxShared);                                                \
+  k_gram_ff<NB, NS><<<grid, DBLK, smem, d.st>>>(A, m, d.sUf, B, d.N, d.rows_per_cta, T, d.part, skip);
+#define QP_GRAMF_CASE(NS)          \
+  case NS:                         \
+    if (two) {                     \
+      QP_GRAMF_LAUNCH(2 * NS, NS)  \
+    } else {                       \
+      QP_GRAMF_LAUNCH(NS, NS)      \
+    }                              \
     break;
-  // the 48 KB default counts the static red[] too, so every size is opted in
   switch (d.nsd) {
     QP_GRAMF_CASE(1)
     QP_GRAMF_CASE(2)
@@ -1105,6 +1098,7 @@ int gram_ff(Dav& d, const float2* A, int m, const float2* B, int nbc, double* ou
       return -1;
   }
 #undef QP_GRAMF_CASE
+#undef QP_GRAMF_LAUNCH
   k_reduce_partials<<<gsz((int64_t)m * nbc * 32), DBLK, 0, d.st>>>(d.part, d.ncta, m * nbc, out, skip);
   return 0;
 }
