@@ -19,14 +19,16 @@
 // the first iteration of each restart cycle, which runs the FP64 sigma on the
 // re-contracted Ritz vectors (defect correction).  Convergence is accepted only
 // on an FP64 iteration; an FP32 iteration that meets the threshold forces a
-// restart, so the reported energies and residuals are FP64 ones.  With
-// QPGPU_FF the restart sigma is the float-float one (k_sigma_ff, FP64-class
-// accuracy on the FP32 pipes) and convergence is accepted on those iterations.
-// In both mixed modes the tall-skinny algebra (Gram blocks of the
-// Gram-Schmidt passes and projections, the updates, Ritz vectors and
-// re-contraction) runs in float-float on the FP32 pipes (k_gram<., true>,
-// k_lincomb_ff); the small factorisations, the eigenproblem, the step and
-// the residual norms stay FP64.
+// restart, so the reported energies are FP64 ones.  With QPGPU_FF the restart
+// sigma is the float-float one (k_sigma_ff, FP64-class accuracy on the FP32
+// pipes) and convergence is accepted on those iterations.  In both mixed
+// modes the tall-skinny algebra runs on the FP32 pipes: the Gram blocks of
+// the Gram-Schmidt passes and projections (k_gram_ff on float-float copies
+// of the blocks), the updates, the restart iterations' Ritz vectors and the
+// re-contraction in float-float (k_lincomb_ff); the Ritz vectors of
+// FP32-sigma iterations in FP32 (k_lincomb32); the step's preconditioner and
+// norms in FP32 after an FP64 residual numerator (k_step_mixed).  The small
+// factorisations and the eigenproblem stay FP64.
 #include <algorithm>
 #include <cmath>
 #include <cstring>
@@ -501,10 +503,10 @@ __global__ void __launch_bounds__(DBLK) k_lincomb(LinComb L, int nb, int64_t N, 
 // FP32 FMAs for each FP64 FMA): each product of split operands is formed
 // exactly for hi*hi (an FMA gives its rounding error) plus the hi*lo cross
 // terms, and the running sum is kept as an unevaluated pair with Knuth's
-// TwoSum on the high part.  About 47-bit accuracy; used for the Ritz vectors
-// U y, W y, S y of the mixed-precision Davidson, whose W and S come from the
-// FP32 sigma on most iterations.  Same row ownership, loads and summation
-// order as k_lincomb.
+// TwoSum on the high part.  About 47-bit accuracy; used by the
+// mixed-precision Davidson for the Gram-Schmidt / Cholesky-QR updates, the
+// Ritz vectors of restart iterations and the re-contraction.  Same row
+// ownership, loads and summation order as k_lincomb.
 template <int NSD>
 __global__ void __launch_bounds__(DBLK) k_lincomb_ff(LinComb L, int nb, int64_t N, const double* C, const int* skip) {
   if (skip && *skip) return;
