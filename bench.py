@@ -58,6 +58,8 @@ def parse():
     ap.add_argument("--batch", action="store_true",
                     help="add the batched block: 64 independent CI problems solved together vs one by one")
     ap.add_argument("--batch-only", action="store_true", help="only the batched block")
+    ap.add_argument("--c1", action="store_true",
+                    help="only the 1e4-determinant, 40-MO Davidson: device vs the oracle's CPU Davidson")
     ap.add_argument("--n-states-diag", type=int, default=8, help="N_st_diag of the Davidson runs")
     ap.add_argument("--davidson-sze-max", type=int, default=10, help="davidson_sze_max of the Davidson runs")
     return ap.parse_args()
@@ -291,6 +293,45 @@ def davidson_block(prob, wf):
     return out
 
 
+def c1_block(nsd=4, sze_max=10, threshold=1e-10):
+    """10 alpha + 10 beta electrons in 40 MOs (N_int = 1), 1e4 seeded determinants, 1 state:
+    the device Davidson (FP64, mixed) against the oracle's CPU Davidson (the C++ restatement of
+    davidson_diag_hjj_sjj over the OpenMP sigma, all host threads), same guess and threshold.
+    The device runs report time-to-E (first FP64 iteration within 1e-6 Ha of the converged
+    energy) and total time; the CPU run reports its total time to the threshold."""
+    from quantum_package_gb300 import FP32, FP64
+    from quantum_package_gb300 import generate as G
+    from quantum_package_gb300.sigma import Wavefunction
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    from oracle import Oracle
+    prob = G.make_problem(1)
+    N = prob.n_det
+    rng = np.random.default_rng(prob.seed)
+    u = rng.normal(size=(nsd, N))
+    u[0] = 0.0
+    u[0, 0] = 1.0
+    o = Oracle.from_problem(prob)
+    t = time.perf_counter()
+    eo, _, _, n_sigma_cpu, res_cpu = o.davidson(u, 1, davidson_sze_max=sze_max, threshold=threshold, s2_eig=False,
+                                                 max_sigma=1000)
+    cpu_s = time.perf_counter() - t
+    wf = Wavefunction.from_problem(prob)
+    kw = dict(n_states=1, s2_eig=False, max_iter=1000, davidson_sze_max=sze_max)
+    e_ref = np.asarray(eo[:1])
+    out = {"workload": "Davidson, 10a+10b in 40 MOs (N_int=1), 1e4 seeded dets, 1 state",
+           "n_states_diag": nsd, "davidson_sze_max": sze_max, "threshold": threshold,
+           "cpu_oracle": {"total_s": cpu_s, "n_sigma": int(n_sigma_cpu), "energy": float(eo[0]),
+                          "threads": os.cpu_count()}}
+    for name, prec in (("device_fp64", FP64), ("device_mixed", FP32)):
+        wf.davidson_diag_hs2(u, threshold=threshold, precision=prec, **kw)  # warm-up (module load, tuning)
+        r = wf.davidson_diag_hs2(u, threshold=threshold, precision=prec, **kw)
+        t_e, it = _time_to_e(r, e_ref, FP64)
+        out[name] = {"time_to_E_s": t_e / 1e3 if t_e is not None else None, "iterations_to_E": it,
+                     "total_s": float(r["trace"]["elapsed_ms"][-1]) / 1e3, "n_sigma": r["n_sigma"],
+                     "converged": r["converged"], "dE_vs_cpu_ha": float(abs(r["energies"][0] - eo[0]))}
+    return out
+
+
 def batch_block(n_problems=64):
     """64 independent CI problems (30-60 MOs, 8-16 electrons per spin, N_det
     log-uniform 1e3-1e5, 1-3 states, seeded): the batched Davidson (one
@@ -361,6 +402,10 @@ def run_ours(args):
     if args.batch_only:
         if rank == 0:
             print(json.dumps({"batch": batch_block()}), flush=True)
+        return 0
+    if args.c1:
+        if rank == 0:
+            print(json.dumps({"c1": c1_block()}), flush=True)
         return 0
     prob = G.make_problem(2, n_det=args.n_det, n_states=N_STATES)
     N = prob.n_det
