@@ -23,9 +23,11 @@ def test_full_ci_dense_matrices(name):
     d = load(name)
     o = _oracle(d)
     H, S = o.dense()
-    # i_H_j generic path == second quantisation, elementwise
+    # i_H_j generic path == second quantisation, elementwise; both operators Hermitian
     np.testing.assert_allclose(H, d["H"], rtol=0, atol=1e-12)
     np.testing.assert_array_equal(S, d["S"])
+    np.testing.assert_allclose(H, H.T, rtol=0, atol=1e-13 * np.abs(H).max())
+    np.testing.assert_array_equal(S, S.T)
     # sigma path (u0Hu0.irp.f) == dense H
     u = np.random.default_rng(1).normal(size=(3, len(d["dets"])))
     v, s = o.h_s2_u0(u)
@@ -80,3 +82,23 @@ def test_sampled_pairs_spin_routines():
         ph, exc, h2, s2 = o.pair_excitation(pos[di.tobytes()], pos[dj.tobytes()], int(k))
         assert abs(h2 - hij) <= 1e-12 * max(1.0, abs(hij))
         assert s2 == sij
+
+
+@pytest.mark.parametrize("name", ["fci_s2", "fci_cs"])
+def test_oracle_davidson_matches_dense_eigenvalues(name):
+    """The oracle's restatement of davidson_diag_hjj_sjj (s2_eig on, spin-complete space)
+    against the eigenvalues of the second-quantisation matrix with the target S^2."""
+    d = load(name)
+    o = _oracle(d)
+    n = len(d["dets"])
+    rng = np.random.default_rng(5)
+    u = rng.normal(size=(4, n))
+    u[0] = 0.0
+    u[0, 0] = 1.0
+    e, s2, _, n_sigma, res = o.davidson(u, 2, threshold=1e-14, s2_eig=True, max_sigma=300)
+    sz = 0.5 * (d["n_alpha"] - d["n_beta"])
+    good = np.abs(d["s2"] - sz * (sz + 1)) < 0.6
+    ref = d["eigvals"][good][:2]
+    assert 0 < n_sigma < 300 and max(res) < 1e-14
+    np.testing.assert_allclose(e[:2], ref, rtol=0, atol=1e-9)
+    np.testing.assert_allclose(s2[:2], sz * (sz + 1), rtol=0, atol=1e-6)
