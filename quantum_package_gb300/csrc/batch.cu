@@ -1,8 +1,8 @@
 // Batched CI problems: many independent determinant sets (each its own
 // qpgpu_ctx) solved together.  Quantum Package solves one problem per
 // process; callers that need many small CI solves (state-specific or
-// multi-reference loops, the batched configuration of this build) would run
-// them one after the other.  Here:
+// multi-reference loops, many small selected spaces) would run them one
+// after the other.  Here:
 //  * sigma for all problems is ONE persistent launch: every warp pulls
 //    (problem, row chunk) work items from a global atomic queue that spans
 //    the whole batch, so problems of uneven size (1e3..1e5 determinants)

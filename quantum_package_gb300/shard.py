@@ -12,8 +12,8 @@ round-robin, compute them with a row-range sigma callable (on a GB300 the
 C-ABI's qpgpu_h_s2_u0_work), and one all_reduce sums the row-disjoint
 results, so every rank ends with the whole v_t and s_t.  A rank that fails or
 leaves is detected by the process group (closed connection or timeout) and
-reported as ShardError instead of a hang.  Each box of this build has one GPU,
-so the multi-rank path is exercised with gloo ranks on the CPU.
+reported as ShardError instead of a hang.  The multi-rank logic is exercised
+with gloo ranks on the CPU (tests/test_shard_gloo.py).
 """
 from __future__ import annotations
 
