@@ -172,6 +172,11 @@ class Wavefunction:
         """davidson_diag_hs2 (diagonalization_hs2.irp.f:1-49) on this determinant set.
 
         u_in: (N_st_diag, N) guess vectors (all of them, seeded by the caller).
+        precision=FP64 is the reference's loop in FP64; FP32 runs the FP32
+        sigma with an FP64 sigma at each restart (defect correction), FF the
+        same with a float-float restart sigma; both mixed modes run the
+        projections and Gram-Schmidt in float-float, accept convergence only
+        on restart iterations and report FP64-accurate energies.
         preconditioner=1 uses the learned step (see mlp_*) in place of the
         diagonal one; preconditioner=2 adds it as an extra direction (in the
         correction slot of Ritz vector n_states + k); collect_every > 0
