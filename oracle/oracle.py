@@ -59,6 +59,8 @@ def lib():
         L.qpo_davidson.argtypes = [C.c_void_p, _dp, C.c_int64, _dp, _dp, C.c_int, C.c_int, C.c_int,
                                    C.c_double, C.c_int, C.c_int, _dp]
         L.qpo_num_threads.restype = C.c_int
+        L.qpo_select_pt2.argtypes = [C.c_void_p, _dp, C.c_int, _dp, C.c_int, C.c_int, C.c_int, _dp, _u64p, _dp,
+                                     C.POINTER(C.c_int64)]
         _lib = L
     return _lib
 
@@ -221,6 +223,61 @@ class Oracle:
         if rc < 0:
             raise RuntimeError(f"qpo_davidson failed ({rc})")
         return e, s2, u, rc, res
+
+    def select_pt2(self, coef, e0, n_gen, n_sel, buf_size):
+        """CIPSI selection with the second-order energy (selection.irp.f restated).
+
+        The context's determinants must be in psi_det_sorted order (sort_by_weight);
+        coef: (n_st, N) in that order, e0: (n_st,) denominators, generators and
+        selectors the first n_gen / n_sel determinants.  Returns (pt2 (n_st,),
+        buffer determinants (n, 2, N_int), buffer values (n,) ascending, number of
+        external determinants with a non-zero numerator)."""
+        coef = np.atleast_2d(np.asarray(coef, dtype=np.float64))
+        n_st = coef.shape[0]
+        cm = np.ascontiguousarray(coef)  # (n_st, N) row-major == (N, n_st) column-major
+        e0 = np.ascontiguousarray(np.atleast_1d(e0), dtype=np.float64)
+        pt2 = np.zeros(n_st)
+        nint = (self.n_mo + 63) // 64
+        dets = np.zeros((max(buf_size, 1), 2, nint), np.uint64)
+        vals = np.zeros(max(buf_size, 1))
+        n_ext = C.c_int64(0)
+        n = lib().qpo_select_pt2(self._h, cm.ravel(), n_st, e0, int(n_gen), int(n_sel), int(buf_size), pt2,
+                                 dets.ravel(), vals, C.byref(n_ext))
+        if n < 0:
+            raise ValueError("qpo_select_pt2: bad arguments")
+        return pt2, dets[:n].copy(), vals[:n].copy(), n_ext.value
+
+
+def sort_by_weight(coef, weights=None):
+    """psi_det_sorted (determinants.irp.f:228-293): the order of determinants
+    by decreasing state-averaged norm contribution sum_k w_k c_ik^2
+    (normalised to 1), coef (n_states, N).  Returns (order, sorted
+    contributions)."""
+    coef = np.atleast_2d(coef)
+    w = np.ones(coef.shape[0]) if weights is None else np.asarray(weights, dtype=np.float64)
+    contrib = (coef * coef * (w + 1e-31)[:, None]).sum(axis=0)
+    contrib = contrib / contrib.sum()
+    order = np.argsort(-contrib, kind="stable")
+    return order, contrib[order]
+
+
+def n_generators(contrib_sorted, threshold=0.99):
+    """N_det_generators of Generators_full (generators.irp.f:3-22): the first
+    determinants whose cumulative contribution reaches threshold."""
+    c = np.cumsum(contrib_sorted)
+    hit = np.nonzero(c >= threshold)[0]
+    return max(int(hit[0]) + 1 if len(hit) else len(c), 1)
+
+
+def n_selectors(contrib_sorted, n_gen, threshold=0.999, threshold_generators=0.99):
+    """N_det_selectors of Selectors_full (selectors.irp.f:3-25)."""
+    n = len(contrib_sorted)
+    if threshold_generators < 1.0:
+        c = np.cumsum(contrib_sorted)
+        hit = np.nonzero(c > threshold)[0]
+        n = int(hit[0]) + 1 if len(hit) else n
+        n = max(n, n_gen)
+    return n
 
 
 def num_threads() -> int:

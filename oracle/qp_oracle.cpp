@@ -17,12 +17,15 @@
 // the quantum_package source tree).  FP contraction is disabled at build time
 // (-ffp-contract=off) so results are identical on x86-64 and aarch64.
 #include <algorithm>
+#include <array>
 #include <cmath>
 #include <cstdint>
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
 #include <numeric>
+#include <unordered_map>
+#include <unordered_set>
 #include <vector>
 #ifdef _OPENMP
 #include <omp.h>
@@ -1293,5 +1296,277 @@ int qpo_pair_excitations(qpo_ctx* hc, int64_t n, const int32_t* I, const int32_t
     if (ph == -1 || ph == 1) phase[i] = (int8_t)ph; else bad = 1;
   }
   return bad ? -1 : 0;
+}
+}
+
+// ---------------------------------------------------------------------------
+// CIPSI selection with the Epstein-Nesbet second-order energy
+// (plugins/Full_CI_ZMQ/selection.irp.f), restated on the determinant level.
+//
+// The reference walks, for each generator (the first N_det_generators
+// determinants of psi_det_sorted), every pair of holes and every pair of
+// particles, and for each external determinant a (a single or double
+// excitation of the generator, not in the wave function):
+//   * skips a when it is within a double excitation of an earlier generator
+//     (spot_isinwf fullMatch, past_d1, past_d2: :1088-1172), so every external
+//     determinant is counted once, by the first generator that reaches it;
+//   * skips a when it is in the wave function (spot_isinwf banned, :1130-1172);
+//   * forms mat(st) = sum over selectors D of c_D,st <a|H|D> (splash_pq,
+//     get_d0/d1/d2: :647-1086), skipping a when every mat(st) is zero;
+//   * H_aa = diag_H_mat_elem_fock(generator, a) (slater_rules.irp.f:1800-1866)
+//     from the generator's build_fock_tmp (Fock_diag.irp.f:1-98);
+//   * e(st) = (sign(delta) sqrt(delta^2 + (2 mat)^2) - delta) / 2 with
+//     delta = E0(st) - H_aa, pt2(st) += e(st), and the buffer receives
+//     a with the value min(0, min_st e(st)) (fill_buffer_double, :582-645);
+//     the buffer keeps the most negative values (selection_buffer.irp.f:33-138).
+// Here the same set of external determinants is enumerated generator by
+// generator (a hash set stands in for the banned masks), <a|H|D> comes from
+// the generic i_H_j path, and each external's numerator is summed over the
+// selectors in their order.
+// ---------------------------------------------------------------------------
+namespace {
+
+typedef std::array<u64, 4> DetKey;  // (alpha words, beta words), N_int <= 2
+
+struct DetKeyHash {
+  size_t operator()(const DetKey& k) const {
+    u64 h = 0x9e3779b97f4a7c15ull;
+    for (u64 w : k) {
+      h ^= w + 0x9e3779b97f4a7c15ull + (h << 6) + (h >> 2);
+      h *= 0xbf58476d1ce4e5b9ull;
+    }
+    return (size_t)(h ^ (h >> 31));
+  }
+};
+
+DetKey make_key(const u64* d, int nint) {
+  DetKey k{};
+  for (int i = 0; i < 2 * nint; ++i) k[i] = d[i];
+  return k;
+}
+
+inline void flip_bit(u64* d, int nint, int spin, int orb) {  // orb 1-based, spin 0/1
+  d[spin * nint + ((orb - 1) >> 6)] ^= u64(1) << ((orb - 1) & 63);
+}
+
+// every single and double excitation of det g (both spins), fn(const u64* a)
+template <class Fn>
+void for_each_excitation(const Ctx& c, const u64* g, Fn&& fn) {
+  const int nint = c.nint, n = c.n_mo;
+  int occ[2][256], vir[2][256], no[2], nv[2];
+  for (int s = 0; s < 2; ++s) {
+    no[s] = to_list(g + s * nint, nint, occ[s]);
+    nv[s] = 0;
+    for (int o = 1; o <= n; ++o)
+      if (!((g[s * nint + ((o - 1) >> 6)] >> ((o - 1) & 63)) & 1)) vir[s][nv[s]++] = o;
+  }
+  u64 a[8];
+  auto reset = [&]() { std::memcpy(a, g, sizeof(u64) * 2 * nint); };
+  for (int s = 0; s < 2; ++s)
+    for (int i = 0; i < no[s]; ++i)
+      for (int j = 0; j < nv[s]; ++j) {
+        reset();
+        flip_bit(a, nint, s, occ[s][i]);
+        flip_bit(a, nint, s, vir[s][j]);
+        fn(a);
+      }
+  for (int s = 0; s < 2; ++s)
+    for (int i1 = 0; i1 < no[s]; ++i1)
+      for (int i2 = i1 + 1; i2 < no[s]; ++i2)
+        for (int j1 = 0; j1 < nv[s]; ++j1)
+          for (int j2 = j1 + 1; j2 < nv[s]; ++j2) {
+            reset();
+            flip_bit(a, nint, s, occ[s][i1]);
+            flip_bit(a, nint, s, occ[s][i2]);
+            flip_bit(a, nint, s, vir[s][j1]);
+            flip_bit(a, nint, s, vir[s][j2]);
+            fn(a);
+          }
+  for (int i1 = 0; i1 < no[0]; ++i1)
+    for (int j1 = 0; j1 < nv[0]; ++j1)
+      for (int i2 = 0; i2 < no[1]; ++i2)
+        for (int j2 = 0; j2 < nv[1]; ++j2) {
+          reset();
+          flip_bit(a, nint, 0, occ[0][i1]);
+          flip_bit(a, nint, 0, vir[0][j1]);
+          flip_bit(a, nint, 1, occ[1][i2]);
+          flip_bit(a, nint, 1, vir[1][j2]);
+          fn(a);
+        }
+}
+
+// build_fock_tmp, Fock_diag.irp.f:1-98: f[s * (n_mo + 2) + i], i = 1..n_mo, and
+// f[s * (n_mo + 2) + n_mo + 1] = <g|H|g>
+void build_fock_tmp(const Ctx& c, const u64* g, std::vector<double>& f) {
+  const int n = c.n_mo, st = n + 2;
+  f.assign(2 * (size_t)st, 0.0);
+  int occ[2][256];
+  to_list(g, c.nint, occ[0]);
+  to_list(g + c.nint, c.nint, occ[1]);
+  double e0 = 0.0;
+  for (int ii = 0; ii < c.na; ++ii) {
+    const int i = occ[0][ii];
+    f[i] += c.H(i, i);
+    e0 += c.H(i, i);
+    for (int jj = 0; jj < c.na; ++jj) {
+      const int j = occ[0][jj];
+      if (i == j) continue;
+      f[i] += c.JA(i, j);
+      e0 += 0.5 * c.JA(i, j);
+    }
+    for (int jj = 0; jj < c.nb; ++jj) {
+      const int j = occ[1][jj];
+      f[i] += c.JJ(i, j);
+      e0 += c.JJ(i, j);
+    }
+  }
+  for (int ii = 0; ii < c.nb; ++ii) {
+    const int i = occ[1][ii];
+    f[st + i] += c.H(i, i);
+    e0 += c.H(i, i);
+    for (int jj = 0; jj < c.nb; ++jj) {
+      const int j = occ[1][jj];
+      if (i == j) continue;
+      f[st + i] += c.JA(i, j);
+      e0 += 0.5 * c.JA(i, j);
+    }
+    for (int jj = 0; jj < c.na; ++jj) f[st + i] += c.JJ(i, occ[0][jj]);
+  }
+  for (int i = 1; i <= n; ++i) {  // virtual MOs
+    if (f[i] != 0.0) continue;
+    f[i] += c.H(i, i);
+    for (int jj = 0; jj < c.na; ++jj) f[i] += c.JA(i, occ[0][jj]);
+    for (int jj = 0; jj < c.nb; ++jj) f[i] += c.JJ(i, occ[1][jj]);
+  }
+  for (int i = 1; i <= n; ++i) {
+    if (f[st + i] != 0.0) continue;
+    f[st + i] += c.H(i, i);
+    for (int jj = 0; jj < c.nb; ++jj) f[st + i] += c.JA(i, occ[1][jj]);
+    for (int jj = 0; jj < c.na; ++jj) f[st + i] += c.JJ(i, occ[0][jj]);
+  }
+  f[n + 1] = e0;
+  f[st + n + 1] = e0;
+}
+
+// diag_H_mat_elem_fock, slater_rules.irp.f:1800-1866 (pert within a double
+// excitation of ref)
+double diag_h_fock(const Ctx& c, const u64* ref, const u64* pert, const std::vector<double>& f) {
+  const int n = c.n_mo, st = n + 2;
+  auto F = [&](int s, int i) { return f[(size_t)(s - 1) * st + i]; };
+  const double e0 = F(1, n + 1);
+  const int degree = exc_degree(ref, pert, c.nint);
+  if (degree == 2) {
+    int exc[2][2][2], nexc[2][2];
+    double phase;
+    double_exc_generic(ref, pert, c.nint, exc, nexc, &phase);
+    int h1, h2, p1, p2, s1, s2;
+    if (nexc[0][0] == 2) {  // decode_exc, slater_rules.irp.f:105-160
+      h1 = exc[0][0][0]; h2 = exc[0][0][1]; p1 = exc[0][1][0]; p2 = exc[0][1][1]; s1 = s2 = 1;
+    } else if (nexc[1][0] == 2) {
+      h1 = exc[1][0][0]; h2 = exc[1][0][1]; p1 = exc[1][1][0]; p2 = exc[1][1][1]; s1 = s2 = 2;
+    } else {
+      h1 = exc[0][0][0]; h2 = exc[1][0][0]; p1 = exc[0][1][0]; p2 = exc[1][1][0]; s1 = 1; s2 = 2;
+    }
+    if (s1 == s2)
+      return e0 - F(s1, h1) + (F(s1, p1) - c.JA(h1, p1)) - (F(s1, h2) - c.JA(h1, h2) + c.JA(p1, h2)) +
+             (F(s1, p2) - c.JA(h1, p2) + c.JA(p1, p2) - c.JA(h2, p2));
+    return e0 - F(1, h1) + (F(1, p1) - c.JA(h1, p1)) - (F(2, h2) - c.JJ(h1, h2) + c.JJ(p1, h2)) +
+           (F(2, p2) - c.JJ(h1, p2) + c.JJ(p1, p2) - c.JA(h2, p2));
+  }
+  if (degree == 1) {
+    int h, p, spin;
+    double phase;
+    mono_exc_generic(ref, pert, c.nint, &h, &p, &spin, &phase);
+    return e0 - F(spin, h) + (F(spin, p) - c.JA(h, p));
+  }
+  return e0;
+}
+
+struct SelCand {
+  double val;
+  DetKey key;
+};
+
+}  // namespace
+
+extern "C" {
+// Selection over the wave function held by the context, whose determinants
+// must be in psi_det_sorted order: generators = determinants 0..n_gen-1,
+// selectors = 0..n_sel-1 (n_gen <= n_sel <= N).  coef(N, n_st) column-major
+// (psi_coef_sorted), e0(n_st) the denominators (pt2_E0_denominator).  Writes
+// pt2(n_st), the buf_size most negative buffer values (ascending, ties in
+// determinant-bit order) with their determinants (N_int, 2) each, and the
+// number of external determinants with a non-zero numerator.  Returns the
+// number of buffer entries written, or -1 on bad arguments.
+int qpo_select_pt2(qpo_ctx* hc, const double* coef, int n_st, const double* e0, int n_gen, int n_sel, int buf_size,
+                   double* pt2, uint64_t* buf_dets, double* buf_vals, int64_t* n_ext) {
+  if (!hc || !coef || !e0 || !pt2) return -1;
+  const Ctx& c = *reinterpret_cast<Ctx*>(hc);
+  const int64_t N = c.N;
+  const int nint = c.nint;
+  if (n_st < 1 || n_gen < 1 || n_gen > n_sel || n_sel > N || nint > 2 || buf_size < 0 ||
+      (buf_size > 0 && (!buf_dets || !buf_vals)))
+    return -1;
+  std::unordered_set<DetKey, DetKeyHash> inwf;
+  inwf.reserve((size_t)N * 2);
+  for (int64_t i = 0; i < N; ++i) inwf.insert(make_key(c.det(i), nint));
+  // external determinants in order of their (first) generator
+  std::unordered_map<DetKey, int64_t, DetKeyHash> ext_index;
+  std::vector<DetKey> ext;
+  std::vector<int> ext_gen;
+  for (int g = 0; g < n_gen; ++g)
+    for_each_excitation(c, c.det(g), [&](const u64* a) {
+      DetKey k = make_key(a, nint);
+      if (inwf.count(k) || ext_index.count(k)) return;
+      ext_index.emplace(k, (int64_t)ext.size());
+      ext.push_back(k);
+      ext_gen.push_back(g);
+    });
+  // numerators: sum over the selectors, in their order
+  std::vector<double> v(ext.size() * (size_t)n_st, 0.0);
+  for (int D = 0; D < n_sel; ++D)
+    for_each_excitation(c, c.det(D), [&](const u64* a) {
+      auto it = ext_index.find(make_key(a, nint));
+      if (it == ext_index.end()) return;
+      const double hij = i_h_j(c, a, c.det(D));
+      for (int s = 0; s < n_st; ++s) v[(size_t)it->second * n_st + s] += coef[D + (size_t)N * s] * hij;
+    });
+  for (int s = 0; s < n_st; ++s) pt2[s] = 0.0;
+  std::vector<SelCand> cand;
+  std::vector<double> f;
+  int fg = -1;
+  int64_t nz = 0;
+  for (size_t i = 0; i < ext.size(); ++i) {
+    double sabs = 0.0;
+    for (int s = 0; s < n_st; ++s) sabs += std::fabs(v[i * n_st + s]);
+    if (sabs == 0.0) continue;
+    ++nz;
+    const int g = ext_gen[i];
+    if (g != fg) {
+      build_fock_tmp(c, c.det(g), f);
+      fg = g;
+    }
+    const double haa = diag_h_fock(c, c.det(g), ext[i].data(), f);
+    double mine = 0.0;
+    for (int s = 0; s < n_st; ++s) {
+      const double delta = e0[s] - haa;
+      const double val = v[i * n_st + s] + v[i * n_st + s];
+      double tmp = std::sqrt(delta * delta + val * val);
+      if (delta < 0.0) tmp = -tmp;
+      const double e = 0.5 * (tmp - delta);
+      pt2[s] += e;
+      mine = std::min(e, mine);
+    }
+    cand.push_back({mine, ext[i]});
+  }
+  if (n_ext) *n_ext = nz;
+  const size_t nout = std::min(cand.size(), (size_t)buf_size);
+  auto less = [](const SelCand& x, const SelCand& y) { return x.val < y.val || (x.val == y.val && x.key < y.key); };
+  std::partial_sort(cand.begin(), cand.begin() + nout, cand.end(), less);
+  for (size_t i = 0; i < nout; ++i) {
+    buf_vals[i] = cand[i].val;
+    for (int w = 0; w < 2 * nint; ++w) buf_dets[i * 2 * nint + w] = cand[i].key[w];
+  }
+  return (int)nout;
 }
 }
