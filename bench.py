@@ -17,9 +17,14 @@ e2e        FP64 sigma through qpgpu_h_s2_u0 with host (pinned) buffers,
 sigma_fp32 FP32 matrix elements x FP32 coefficients with Kahan sums
 roofline   dominant kernel k_sigma64: algorithmic bytes per launch
            B = N*N_st*8*3 + N*(2*N_int*8+12) + P*N_st*8 over its CUDA-event time
-cpu_baseline  the CPU oracle (C++ restatement of H_S2_u_0_nstates_openmp_work,
-           OpenMP, all host threads) on a strided row sample of the same workload
---impl reference: that CPU path alone, as the reference arm.
+cpu_baseline  the CPU oracle (C++ restatement of H_S2_u_0_nstates_openmp,
+           OpenMP dynamic,64, all host threads): one full sigma of all N_det rows
+           in bilinear order for the 4 states (the converged Davidson vectors when
+           the Davidson block runs; its output gives the oracle energies)
+davidson   time-to-E of each arm against the oracle's FP64 energies: the
+           Rayleigh quotients of the oracle's sigma on the converged vectors
+--impl reference: that CPU path alone, as the reference arm, each step a
+           contiguous block of bilinear rows (the blocks of all steps tile the set).
 """
 from __future__ import annotations
 
@@ -48,8 +53,6 @@ def parse():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--n-det", type=int, default=1_000_000)
-    ap.add_argument("--cpu-sample-step", type=int, default=10,
-                    help="row stride of the CPU-oracle sample (1/step of the rows, about 10-15 s on 16 cores)")
     ap.add_argument("--reference-budget-s", type=float, default=150.0,
                     help="wall-time budget of the whole --impl reference run (warm-up + timed steps)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
@@ -146,21 +149,45 @@ def profiled_traffic(N, P):
         return None, None
 
 
-def cpu_sample(prob, step, nst=N_STATES, repeat=1):
-    """CPU oracle sigma on rows 1, 1+step, ...: returns (det*state/s, seconds, rows, threads)."""
+def cpu_model():
+    """CPU model name of this host (lscpu, else /proc/cpuinfo)."""
+    try:
+        out = subprocess.run(["lscpu"], capture_output=True, text=True, timeout=10).stdout
+        for ln in out.splitlines():
+            if ln.startswith("Model name:"):
+                return ln.split(":", 1)[1].strip()
+    except (OSError, subprocess.SubprocessError):
+        pass
+    try:
+        with open("/proc/cpuinfo") as f:
+            for ln in f:
+                if ln.lower().startswith("model name"):
+                    return ln.split(":", 1)[1].strip()
+    except OSError:
+        pass
+    return "unknown"
+
+
+def oracle_full_sigma(prob, u):
+    """The CPU oracle's sigma on all N_det rows of u (N_st, N) in psi_det order:
+    returns (v, s, seconds, threads, oracle).  The determinant index (the
+    providers) is built before the clock starts, as the GPU set-up is."""
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     from oracle import Oracle, num_threads
     o = Oracle.from_problem(prob)
-    from quantum_package_gb300 import generate as G
-    u_t = np.ascontiguousarray(G.random_coefficients(prob.n_det, nst, prob.seed).T)
-    rows = len(range(0, prob.n_det, step))
-    best = None
-    for _ in range(repeat):
-        t = time.perf_counter()
-        o.h_s2_u0_work(u_t, 1, prob.n_det, 0, step)
-        dt = time.perf_counter() - t
-        best = dt if best is None else min(best, dt)
-    return rows * nst / best, best, rows, num_threads(), o
+    t = time.perf_counter()
+    v, s = o.h_s2_u0(u)
+    dt = time.perf_counter() - t
+    return v, s, dt, num_threads(), o
+
+
+def cpu_baseline_entry(n_det, nst, seconds, threads, what):
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    from oracle import build_flags
+    return {"value": n_det * nst / seconds, "unit": UNIT, "cores": threads, "kind": "port",
+            "sample": f"all {n_det} rows (contiguous, bilinear order), {nst} states, one full sigma of {what}: "
+                      f"{seconds:.1f} s",
+            "flags": build_flags(), "cpu_model": cpu_model()}
 
 
 def run_reference(args):
@@ -170,31 +197,42 @@ def run_reference(args):
     from quantum_package_gb300 import generate as G
     prob = G.make_problem(2, n_det=args.n_det, n_states=N_STATES)
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
-    from oracle import Oracle, num_threads
+    from oracle import Oracle, build_flags, num_threads
     o = Oracle.from_problem(prob)
     u_t = np.ascontiguousarray(G.random_coefficients(prob.n_det, N_STATES, prob.seed).T)
-    # per-step sample: a row stride sized so that warm-up + timed steps fit the
-    # budget (calibrated on a 1/1000 sample), never denser than --cpu-sample-step
+    N = prob.n_det
+    # each step is one contiguous block of bilinear rows (so the reference's
+    # kcol_prev reuse of the beta-singles scan works as in a full sigma); the
+    # blocks of the warm-up and timed steps start at evenly spaced rows and
+    # together tile the set, their size bounded so the run fits the budget
+    nblk = max(1, args.steps + args.warmup)
     t = time.perf_counter()
-    o.h_s2_u0_work(u_t, 1, prob.n_det, 0, 1000)
-    rows_per_s = len(range(0, prob.n_det, 1000)) / max(time.perf_counter() - t, 1e-6)
-    per_step_s = args.reference_budget_s / max(1, args.steps + args.warmup)
-    step = max(args.cpu_sample_step, int(np.ceil(prob.n_det / max(1.0, rows_per_s * per_step_s))))
-    rows = len(range(0, prob.n_det, step))
-    for _ in range(args.warmup):
-        o.h_s2_u0_work(u_t, 1, prob.n_det, 0, step)
+    mid = N // 2
+    o.h_s2_u0_work(u_t, mid + 1, min(N, mid + 2000), 0, 1)
+    rows_per_s = min(2000, N - mid) / max(time.perf_counter() - t, 1e-6)
+    per_step_s = args.reference_budget_s / nblk
+    span = (N + nblk - 1) // nblk
+    B = int(max(1, min(span, rows_per_s * per_step_s)))
+    starts = [1 + i * span for i in range(nblk)]
+    for i in range(args.warmup):
+        o.h_s2_u0_work(u_t, starts[i], min(N, starts[i] + B - 1), 0, 1)
+    rows = 0
     t = time.perf_counter()
-    for _ in range(args.steps):
-        o.h_s2_u0_work(u_t, 1, prob.n_det, 0, step)
+    for i in range(args.warmup, nblk):
+        iend = min(N, starts[i] + B - 1)
+        o.h_s2_u0_work(u_t, starts[i], iend, 0, 1)
+        rows += max(0, iend - starts[i] + 1)
     dt = time.perf_counter() - t
-    val = rows * N_STATES * args.steps / dt
-    sample = f"rows 1+{step}k of {prob.n_det} ({rows} rows, {N_STATES} states) per step"
+    val = rows * N_STATES / dt
+    sample = (f"contiguous blocks of {B} bilinear rows starting every {span} rows of {N} "
+              f"({rows} rows over {args.steps} steps, {N_STATES} states)")
     line = {
         "impl": "reference", "metric": METRIC, "value": val, "unit": UNIT, "n_gpus": args.gpus,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": dt / args.steps * 1e3,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
         "config": workload_config(prob),
-        "cpu_baseline": {"value": val, "unit": UNIT, "cores": num_threads(), "kind": "port", "sample": sample},
+        "cpu_baseline": {"value": val, "unit": UNIT, "cores": num_threads(), "kind": "port", "sample": sample,
+                         "flags": build_flags(), "cpu_model": cpu_model()},
         "e2e": {"value": val, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
         "note": "CPU oracle (C++ FP64 restatement of u0Hu0.irp.f:97-448, OpenMP dynamic,64); the Fortran "
                 "reference cannot be compiled here (no gfortran/irpf90)",
@@ -236,8 +274,11 @@ def _time_to_e(res, e_ref, fp64):
 def davidson_block(prob, wf):
     """Time-to-E of the 4 lowest states: plain FP64 Davidson vs mixed precision vs
     mixed precision + learned preconditioner (trained on the first 1e4 and 2e5
-    determinants of the same draw, as earlier CIPSI stages)."""
-    from quantum_package_gb300 import FF, FP32, FP64
+    determinants of the same draw, as earlier CIPSI stages).  Returns the
+    block's settings, the raw runs and the tight FP64 run whose eigenvectors the
+    oracle checks; davidson_finish turns the runs into times against the
+    oracle's energies."""
+    from quantum_package_gb300 import ALGEBRA_FP64, FF, FP32
     N = prob.n_det
     u = _guess(N, prob.seed)
     kw = dict(n_states=N_STATES, s2_eig=False, max_iter=400, davidson_sze_max=SZE_MAX)
@@ -245,24 +286,19 @@ def davidson_block(prob, wf):
     # one-time costs of the FP32 path (module load, launch-shape tuning for this
     # determinant set) outside the timed runs, as the set-up is
     wf.davidson_diag_hs2(u, threshold=1e-10, precision=FP32, **dict(kw, max_iter=3))
-    e_ref = tight["energies"][:N_STATES]
     out = {"n_states": N_STATES, "n_states_diag": N_STATES_DIAG, "davidson_sze_max": SZE_MAX,
            "threshold": 1e-10, "e_tol_ha": E_TOL,
-           "fp64_reference_energies": e_ref.tolist(),
            "note": "s2_eig off: the seeded space is not spin complete; energies are electronic (Ha)"}
+    raw = {}
 
     def run(name, **extra):
-        r = wf.davidson_diag_hs2(u, threshold=1e-10, **kw, **extra)
-        t, it = _time_to_e(r, e_ref, FP64)
-        out[name] = {"time_to_E_s": t / 1e3 if t is not None else None, "iterations_to_E": it,
-                     "n_sigma": r["n_sigma"], "converged": r["converged"],
-                     "total_s": float(r["trace"]["elapsed_ms"][-1]) / 1e3,
-                     "max_dE_ha": float(np.abs(r["energies"][:N_STATES] - e_ref).max()),
-                     "n_fallback": r["n_fallback"]}
-        return r
+        raw[name] = wf.davidson_diag_hs2(u, threshold=1e-10, **kw, **extra)
 
     run("plain_fp64")
     run("mixed", precision=FP32)
+    # the specification's split: FP32 sigma with the FP64 sigma at each restart,
+    # projections, Gram-Schmidt, Ritz vectors, step and residual norms in FP64
+    run("mixed_spec", precision=FP32, algebra=ALGEBRA_FP64)
     # restart (defect-correction) sigma in float-float instead of FP64
     run("mixed_ff_restart", precision=FF)
     # learned preconditioner: earlier stages of the same determinant draw
@@ -287,7 +323,37 @@ def davidson_block(prob, wf):
     run("mixed_learned", precision=FP32, preconditioner=1)
     run("mixed_learned_extra", precision=FP32, preconditioner=2)
     run("mixed_ff_restart_learned_extra", precision=FF, preconditioner=2)
-    for arm in ("mixed", "mixed_ff_restart", "mixed_learned", "mixed_learned_extra", "mixed_ff_restart_learned_extra"):
+    return out, raw, tight
+
+
+def oracle_energies(prob, vecs, v, s, o):
+    """Rayleigh quotients of the oracle's sigma on the vectors vecs (N_st, N),
+    with the residual norms |Hu - Eu| / |u| and the reference's convergence
+    measure (the squared norm of the Davidson step, diagonalization_hs2.irp.f:386-395)."""
+    hjj, _ = o.diag()
+    sz = 0.5 * (prob.n_alpha - prob.n_beta)
+    sz2sz = sz * (sz - 1.0)
+    uu = np.einsum("ij,ij->i", vecs, vecs)
+    e = np.einsum("ij,ij->i", vecs, v) / uu
+    s2 = np.einsum("ij,ij->i", vecs, s) / uu + sz2sz
+    r = v - e[:, None] * vecs
+    res = np.sqrt(np.einsum("ij,ij->i", r, r) / uu)
+    step = (-r) * (1.0 + s2[:, None] * vecs - s - sz2sz) / np.maximum(hjj[None, :] - e[:, None], 1e-2)
+    return e, res, np.einsum("ij,ij->i", step, step)
+
+
+def davidson_finish(out, raw, e_ref):
+    from quantum_package_gb300 import FP64
+    for name, r in raw.items():
+        t, it = _time_to_e(r, e_ref, FP64)
+        out[name] = {"time_to_E_s": t / 1e3 if t is not None else None, "iterations_to_E": it,
+                     "n_sigma": r["n_sigma"], "converged": r["converged"],
+                     "total_s": float(r["trace"]["elapsed_ms"][-1]) / 1e3,
+                     "max_dE_ha": float(np.abs(r["energies"][:N_STATES] - e_ref).max()),
+                     "n_fallback": r["n_fallback"]}
+    for arm in raw:
+        if arm == "plain_fp64":
+            continue
         a, b = out["plain_fp64"]["time_to_E_s"], out[arm]["time_to_E_s"]
         out[f"speedup_{arm}_vs_plain"] = (a / b) if (a and b) else None
     return out
@@ -409,18 +475,13 @@ def run_ours(args):
         return 0
     prob = G.make_problem(2, n_det=args.n_det, n_states=N_STATES)
     N = prob.n_det
-    # CPU baseline before any GPU work (oracle threads)
-    cpu = None
-    if rank == 0 and not args.no_cpu_baseline:
-        val, sec, rows, thr, _ = cpu_sample(prob, args.cpu_sample_step)
-        cpu = {"value": val, "unit": UNIT, "cores": thr, "kind": "port",
-               "sample": f"rows 1+{args.cpu_sample_step}k of {N} ({rows} rows, {N_STATES} states), {sec:.1f} s"}
-
     wf = Wavefunction.from_problem(prob)
     info = wf.info()
     P = info["n_pairs"]
     if args.davidson_only:
-        d = davidson_block(prob, wf)
+        d, raw, tight = davidson_block(prob, wf)
+        d = davidson_finish(d, raw, tight["energies"][:N_STATES])
+        d["e_ref"] = "the tight (1e-12) FP64 device run (--davidson-only skips the oracle)"
         if rank == 0:
             print(json.dumps({"davidson": d, "setup_s": info["setup_ms"] / 1e3}), flush=True)
         return 0
@@ -522,12 +583,34 @@ def run_ours(args):
         "gpu_launches": launches_per_sigma * args.steps,
         "clocks": clk.summary(),
     }
+    dav = raw = tight = None
     if not args.no_davidson:
-        line["davidson"] = davidson_block(prob, wf)
+        dav, raw, tight = davidson_block(prob, wf)
     if args.batch:
         line["batch"] = batch_block()
-    if cpu:
-        line["cpu_baseline"] = cpu
+    # CPU leg after all GPU timing (rank 0): one full oracle sigma of the four
+    # converged FP64 eigenvectors; its time is the CPU baseline, its Rayleigh
+    # quotients the FP64 oracle energies every arm's time-to-E is judged against
+    if rank == 0 and not args.no_cpu_baseline:
+        vecs = tight["vectors"][:N_STATES] if tight is not None else G.random_coefficients(N, N_STATES, prob.seed)
+        ov, os_, sec, thr, o = oracle_full_sigma(prob, vecs)
+        line["cpu_baseline"] = cpu_baseline_entry(
+            N, N_STATES, sec, thr, "the converged Davidson vectors" if tight is not None else "seeded vectors")
+        if dav is not None:
+            e_or, res_or, step_or = oracle_energies(prob, vecs, ov, os_, o)
+            dav = davidson_finish(dav, raw, e_or)
+            dav["oracle_energies"] = e_or.tolist()
+            dav["oracle_residual_norms"] = res_or.tolist()
+            dav["oracle_step_norms2"] = step_or.tolist()
+            dav["gpu_tight_minus_oracle_ha"] = (tight["energies"][:N_STATES] - e_or).tolist()
+            dav["e_ref"] = ("oracle: Rayleigh quotients of the CPU oracle's FP64 sigma on the eigenvectors of a "
+                            "1e-12-converged FP64 device run")
+        del o
+    if dav is not None and "e_ref" not in dav:
+        dav = davidson_finish(dav, raw, tight["energies"][:N_STATES])
+        dav["e_ref"] = "the tight (1e-12) FP64 device run (CPU leg skipped)"
+    if dav is not None:
+        line["davidson"] = dav
     if traffic is not None:
         line["roofline"]["traffic_note"] = tnote
     if rank == 0:

@@ -35,8 +35,11 @@ extern "C" {
 #define QPGPU_ERR_CUDA (-3)     /* CUDA runtime error */
 #define QPGPU_ERR_NOMEM (-4)    /* device allocation failed */
 #define QPGPU_ERR_DAVIDSON (-5) /* Davidson failed (residual > 1e8) */
-#define QPGPU_ERR_TIMEOUT (-6)  /* a bounded device wait ran out */
-#define QPGPU_ERR_NUMERIC (-7)  /* NaN / Inf in an input vector */
+#define QPGPU_ERR_TIMEOUT (-6)  /* reserved for bounded device waits (no entry point waits on a device
+                                   flag in this version, so none returns it) */
+#define QPGPU_ERR_NUMERIC (-7)  /* NaN / Inf in an input vector: checked by the entry points that take
+                                   host arrays (qpgpu_h_s2_u0, _work, qpgpu_u0_h_u0 and the guess of
+                                   qpgpu_davidson_hs2); the asynchronous device entry points do not check */
 
 /* Arithmetic of a sigma application. */
 #define QPGPU_FP64 0  /* FP64 matrix elements and products */
@@ -144,7 +147,10 @@ int qpgpu_sigma_bilinear(qpgpu_ctx* ctx, double* v_t, double* s_t, const double*
  * allocation, for callers that cannot let the library call cudaMalloc (a host
  * code whose device memory belongs to its own pool allocator, or a worker that
  * overlaps sigma with work on other streams and cannot afford the device-wide
- * synchronisation of cudaMalloc/cudaFree).  Same arguments and results.  Its
+ * synchronisation of cudaMalloc/cudaFree).  Same arguments and results as
+ * qpgpu_sigma_bilinear, except that only QPGPU_FP64 and QPGPU_FP32 are accepted
+ * (QPGPU_FF gives QPGPU_ERR_ARG) and the pairs must be stored (a direct-sigma
+ * set gives QPGPU_ERR_STATE).  Its
  * scratch (partial sums of rows split over several work chunks) is a fixed
  * 8 MiB device array of the library, held by every GPU that loads it until
  * exit: the call fails with QPGPU_ERR_ARG when work chunks x n_st exceeds
@@ -171,7 +177,15 @@ typedef struct qpgpu_davidson_params {
   int32_t max_iter;         /* cap on sigma applications (0: 1000) */
   int32_t collect_every;    /* > 0: capture training pairs every k iterations (from the 2nd) */
   int32_t collect_max;      /* captures kept (default 8) */
+  int32_t state_following;  /* state_following (src/Davidson/EZFIO.cfg:19-22): keep the Ritz vectors
+                               that overlap most with the guess states (diagonalization_hs2.irp.f:328-370) */
+  int32_t algebra;          /* mixed modes only: QPGPU_ALGEBRA_FAST runs the projections, Gram-Schmidt,
+                               Ritz vectors and the step on the FP32 pipes (float-float / FP32);
+                               QPGPU_ALGEBRA_FP64 keeps them in FP64 as in the plain loop, so only
+                               sigma runs in FP32 */
 } qpgpu_davidson_params;
+#define QPGPU_ALGEBRA_FAST 0
+#define QPGPU_ALGEBRA_FP64 1
 
 /* Optional per-iteration record of a Davidson run. */
 typedef struct qpgpu_davidson_trace {
@@ -268,6 +282,15 @@ int qpgpu_diag(qpgpu_ctx* ctx, double* h_jj, double* s_jj);
  * total; at most `cap` records are written (pass cap = 0 to query). */
 int qpgpu_connected_pairs(qpgpu_ctx* ctx, int64_t* n_pairs, int32_t* I, int32_t* J, int8_t* cls,
                           int8_t* phase, int16_t* exc, double* hij, int64_t cap);
+
+/* The same export for selected determinants only: the records of
+ * qpgpu_connected_pairs whose I is one of rows[0..n_rows) (0-based psi_det
+ * indices; a repeated index counts once), for spot checks of large sets where
+ * the full list does not fit in host memory.  *n_pairs returns the count; at
+ * most `cap` records are written (cap = 0 queries).  Same routines as above
+ * (slater_rules.irp.f:2783-2987). */
+int qpgpu_connected_pairs_rows(qpgpu_ctx* ctx, const int32_t* rows, int64_t n_rows, int64_t* n_pairs, int32_t* I,
+                               int32_t* J, int8_t* cls, int8_t* phase, int16_t* exc, double* hij, int64_t cap);
 
 #ifdef __cplusplus
 }

@@ -47,6 +47,9 @@ def lib():
         L.qpo_h_s2_u0.argtypes = [C.c_void_p, _dp, _dp, _dp, C.c_int, C.c_int64]
         L.qpo_connected_pairs.argtypes = [C.c_void_p, _i32p, _i32p, _i8p, C.c_int64]
         L.qpo_connected_pairs.restype = C.c_int64
+        L.qpo_h_s2_u0_rows.argtypes = [C.c_void_p, _dp, _dp, _dp, C.c_int, C.c_int64, _i32p, C.c_int64]
+        L.qpo_connected_pairs_rows.argtypes = [C.c_void_p, _i32p, C.c_int64, _i32p, _i32p, _i8p, C.c_int64]
+        L.qpo_connected_pairs_rows.restype = C.c_int64
         L.qpo_pair_excitation.argtypes = [C.c_void_p, C.c_int32, C.c_int32, C.c_int, _i32p,
                                           C.POINTER(C.c_double), C.POINTER(C.c_double)]
         L.qpo_pair_excitations.argtypes = [C.c_void_p, C.c_int64, _i32p, _i32p, _i8p, _i8p, _i32p, _dp, _dp]
@@ -57,7 +60,7 @@ def lib():
         L.qpo_get_s2.restype = C.c_double
         L.qpo_dense.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p]
         L.qpo_davidson.argtypes = [C.c_void_p, _dp, C.c_int64, _dp, _dp, C.c_int, C.c_int, C.c_int,
-                                   C.c_double, C.c_int, C.c_int, _dp]
+                                   C.c_double, C.c_int, C.c_int, _dp, C.c_int]
         L.qpo_num_threads.restype = C.c_int
         L.qpo_select_pt2.argtypes = [C.c_void_p, _dp, C.c_int, _dp, C.c_int, C.c_int, C.c_int, _dp, _u64p, _dp,
                                      C.POINTER(C.c_int64)]
@@ -159,6 +162,34 @@ class Oracle:
             raise ValueError(f"qpo_h_s2_u0_work failed ({rc})")
         return v, s
 
+    def h_s2_u0_rows(self, u0, rows):
+        """Sigma of the determinants `rows` (0-based psi_det) only: u0 (N_st, N) ->
+        (v, s) each (N_st, len(rows)), the worker loops restricted to those rows."""
+        u0 = np.ascontiguousarray(np.atleast_2d(u0), dtype=np.float64)
+        nst, n = u0.shape
+        r = np.ascontiguousarray(rows, dtype=np.int32)
+        v = np.zeros((len(r), nst))
+        s = np.zeros((len(r), nst))
+        rc = lib().qpo_h_s2_u0_rows(self._h, v.ravel(), s.ravel(), u0.ravel(), nst, n, r, len(r))
+        if rc != 0:
+            raise ValueError(f"qpo_h_s2_u0_rows failed ({rc})")
+        return v.T.copy(), s.T.copy()
+
+    def connected_pairs_rows(self, rows):
+        """(I, J, cls) of the pairs of the determinants `rows` (0-based psi_det), sorted by (I, J)."""
+        L = lib()
+        r = np.ascontiguousarray(np.unique(np.asarray(rows)), dtype=np.int32)
+        e32 = np.empty(1, np.int32)
+        n = L.qpo_connected_pairs_rows(self._h, r, len(r), e32, e32, np.empty(1, np.int8), 0)
+        if n < 0:
+            raise ValueError("qpo_connected_pairs_rows: bad rows")
+        I = np.empty(n, np.int32)
+        J = np.empty(n, np.int32)
+        cls = np.empty(n, np.int8)
+        L.qpo_connected_pairs_rows(self._h, r, len(r), I, J, cls, n)
+        o = np.lexsort((J, I))
+        return I[o], J[o], cls[o]
+
     def connected_pairs(self):
         """(I, J, cls) arrays (0-based original order), sorted by (I, J)."""
         L = lib()
@@ -211,7 +242,8 @@ class Oracle:
         lib().qpo_dense(self._h, _ptr(H), _ptr(S))
         return H, S
 
-    def davidson(self, guess, n_states, davidson_sze_max=8, threshold=1e-12, s2_eig=True, max_sigma=500):
+    def davidson(self, guess, n_states, davidson_sze_max=8, threshold=1e-12, s2_eig=True, max_sigma=500,
+                 state_following=False):
         """guess: (N_st_diag, N).  Returns (energies, s2, vectors, n_sigma, residuals)."""
         u = np.ascontiguousarray(guess, dtype=np.float64).copy()
         nsd, n = u.shape
@@ -219,7 +251,7 @@ class Oracle:
         s2 = np.zeros(nsd)
         res = np.zeros(max(n_states, 1))
         rc = lib().qpo_davidson(self._h, u.ravel(), n, e, s2, n_states, nsd, davidson_sze_max,
-                                threshold, int(bool(s2_eig)), max_sigma, res)
+                                threshold, int(bool(s2_eig)), max_sigma, res, int(bool(state_following)))
         if rc < 0:
             raise RuntimeError(f"qpo_davidson failed ({rc})")
         return e, s2, u, rc, res
@@ -282,3 +314,15 @@ def n_selectors(contrib_sorted, n_gen, threshold=0.999, threshold_generators=0.9
 
 def num_threads() -> int:
     return lib().qpo_num_threads()
+
+
+def build_flags() -> str:
+    """CXXFLAGS of the oracle build (oracle/Makefile)."""
+    try:
+        with open(os.path.join(_HERE, "Makefile")) as f:
+            for ln in f:
+                if ln.startswith("CXXFLAGS"):
+                    return ln.split("=", 1)[1].strip()
+    except OSError:
+        pass
+    return "unknown"

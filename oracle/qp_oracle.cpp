@@ -664,8 +664,13 @@ struct PairSink {
 
 // H_S2_u_0_nstates_openmp_work_$N_int, src/Davidson/u0Hu0.irp.f:97-448
 // v_t,s_t,u_t: (N_st, N) in bilinear order; rows istart..iend (1-based)
+// row_list (optional): explicit bilinear rows (1-based, ascending) in place of
+// the range istart+ishift, +istep, ..., <= iend; same loop bodies.
 void sigma_work(const Ctx& c, double* v_t, double* s_t, const double* u_t, int N_st, int istart,
-                int iend, int ishift, int istep, std::vector<std::vector<int64_t>>* pairs_out) {
+                int iend, int ishift, int istep, std::vector<std::vector<int64_t>>* pairs_out,
+                const int* row_list = nullptr, int64_t n_list = 0) {
+  const int64_t n_iter = row_list ? n_list
+                                  : (iend >= istart + ishift ? (int64_t)(iend - istart - ishift) / istep + 1 : 0);
   const int nint = c.nint;
   const int maxab = std::max(c.Ua, c.Ub) + 1;
   int nthreads = 1;
@@ -686,7 +691,8 @@ void sigma_work(const Ctx& c, double* v_t, double* s_t, const double* u_t, int N
     int kcol_prev = -1, n_singles_b = 0;
     // Alpha/Beta double excitations, u0Hu0.irp.f:177-246
 #pragma omp for schedule(dynamic, 64)
-    for (int k_a = istart + ishift; k_a <= iend; k_a += istep) {
+    for (int64_t it = 0; it < n_iter; ++it) {
+      const int k_a = row_list ? row_list[it] : istart + ishift + (int)(it * istep);
       int krow = c.rows[k_a - 1], kcol = c.cols[k_a - 1];
       std::memcpy(tmp_det, c.aun(krow), 8 * nint);
       std::memcpy(tmp_det + nint, c.bun(kcol), 8 * nint);
@@ -726,7 +732,8 @@ void sigma_work(const Ctx& c, double* v_t, double* s_t, const double* u_t, int N
     }
     // Same-spin singles/doubles and diagonal, u0Hu0.irp.f:248-444
 #pragma omp for schedule(dynamic, 64)
-    for (int k_a = istart + ishift; k_a <= iend; k_a += istep) {
+    for (int64_t it = 0; it < n_iter; ++it) {
+      const int k_a = row_list ? row_list[it] : istart + ishift + (int)(it * istep);
       int krow = c.rows[k_a - 1], kcol = c.cols[k_a - 1];
       std::memcpy(tmp_det, c.aun(krow), 8 * nint);
       std::memcpy(tmp_det + nint, c.bun(kcol), 8 * nint);
@@ -1043,6 +1050,66 @@ int64_t qpo_connected_pairs(qpo_ctx* h, int32_t* I, int32_t* J, int8_t* cls, int
   return n;
 }
 
+// Bilinear rows (1-based, ascending) of the psi_det indices psi_rows (0-based).
+static std::vector<int> bilinear_rows(const Ctx& c, const int32_t* psi_rows, int64_t n) {
+  std::vector<int> rl((size_t)n);
+  for (int64_t i = 0; i < n; ++i) rl[i] = c.order_reverse[psi_rows[i]];
+  std::sort(rl.begin(), rl.end());
+  rl.erase(std::unique(rl.begin(), rl.end()), rl.end());
+  return rl;
+}
+
+// Sigma of selected determinants only: the worker loops of
+// u0Hu0.irp.f:177-444 run on the rows of psi_rows (0-based psi_det indices).
+// u0: (n_st, sze) with determinants fastest (u_0(sze,N_st) column-major, psi_det
+// order); v, s: (n, n_st) rows in the order of psi_rows.
+int qpo_h_s2_u0_rows(qpo_ctx* h, double* v, double* s, const double* u0, int n_st, int64_t sze,
+                     const int32_t* psi_rows, int64_t n) {
+  Ctx& c = *reinterpret_cast<Ctx*>(h);
+  const int64_t N = c.N;
+  if (sze < N || n_st < 1 || n < 0) return -1;
+  for (int64_t i = 0; i < n; ++i)
+    if (psi_rows[i] < 0 || psi_rows[i] >= N) return -1;
+  std::vector<double> u_t((size_t)N * n_st), v_t((size_t)N * n_st, 0.0), s_t((size_t)N * n_st, 0.0);
+  for (int k = 0; k < n_st; ++k)
+    for (int64_t i = 0; i < N; ++i) u_t[(size_t)i * n_st + k] = u0[(size_t)k * sze + (c.order[i] - 1)];
+  const std::vector<int> rl = bilinear_rows(c, psi_rows, n);
+  sigma_work(c, v_t.data(), s_t.data(), u_t.data(), n_st, 1, (int)N, 0, 1, nullptr, rl.data(), (int64_t)rl.size());
+  for (int64_t i = 0; i < n; ++i) {
+    const int64_t b = c.order_reverse[psi_rows[i]] - 1;
+    for (int k = 0; k < n_st; ++k) {
+      v[(size_t)i * n_st + k] = v_t[(size_t)b * n_st + k];
+      s[(size_t)i * n_st + k] = s_t[(size_t)b * n_st + k];
+    }
+  }
+  return 0;
+}
+
+// Connected pairs of selected rows (psi_rows, 0-based psi_det indices), as
+// qpo_connected_pairs records them.  Returns the count; fills at most cap.
+int64_t qpo_connected_pairs_rows(qpo_ctx* h, const int32_t* psi_rows, int64_t n, int32_t* I, int32_t* J,
+                                 int8_t* cls, int64_t cap) {
+  Ctx& c = *reinterpret_cast<Ctx*>(h);
+  const int64_t N = c.N;
+  for (int64_t i = 0; i < n; ++i)
+    if (psi_rows[i] < 0 || psi_rows[i] >= N) return -1;
+  std::vector<double> u_t((size_t)N, 0.0), v_t((size_t)N, 0.0), s_t((size_t)N, 0.0);
+  std::vector<std::vector<int64_t>> rec;
+  const std::vector<int> rl = bilinear_rows(c, psi_rows, n);
+  sigma_work(c, v_t.data(), s_t.data(), u_t.data(), 1, 1, (int)N, 0, 1, &rec, rl.data(), (int64_t)rl.size());
+  int64_t m = 0;
+  for (auto& r : rec)
+    for (size_t t = 0; t + 2 < r.size(); t += 3) {
+      if (m < cap) {
+        I[m] = c.order[r[t] - 1] - 1;
+        J[m] = c.order[r[t + 1] - 1] - 1;
+        cls[m] = (int8_t)r[t + 2];
+      }
+      ++m;
+    }
+  return m;
+}
+
 // Excitation data of a connected pair I -> J (0-based original indices), as
 // the spin-specific routines used by the sigma compute it.  exc[0..3] =
 // (h1,p1,h2,p2), 1-based (h2=p2=0 for singles); returns phase (+1/-1).
@@ -1126,7 +1193,7 @@ int qpo_dense(qpo_ctx* h, double* H, double* S2) {
 // N_st_diag entries.  Returns the number of sigma calls (>0) or <0 on error.
 int qpo_davidson(qpo_ctx* hc, double* u_in, int64_t dim_in, double* energies, double* s2_out,
                  int n_st, int n_st_diag, int davidson_sze_max, double threshold, int s2_eig,
-                 int max_sigma, double* res_out) {
+                 int max_sigma, double* res_out, int state_following) {
   Ctx& c = *reinterpret_cast<Ctx*>(hc);
   const int64_t sze = c.N;
   if (n_st_diag * 3 > sze) return -2;  // :110-114
@@ -1215,6 +1282,35 @@ int qpo_davidson(qpo_ctx* hc, double* u_in, int64_t dim_in, double* energies, do
               state_ok[l] = 0;
               break;
             }
+          }
+        }
+      }
+      if (state_following) {  // :328-370, literally (order(k) is a row index used as a column)
+        std::vector<double> ov((size_t)m * m, -1.0);
+        for (int k = 0; k < shift2; ++k)
+          for (int i = 0; i < shift2; ++i) ov[k + (size_t)i * m] = std::fabs(y[k + (size_t)i * m]);
+        std::vector<int> order(n_st);
+        for (int k = 0; k < n_st; ++k) {
+          double cmax = -1.0;
+          for (int i = 0; i < n_st; ++i)
+            if (ov[i + (size_t)k * m] > cmax) {
+              cmax = ov[i + (size_t)k * m];
+              order[k] = i;
+            }
+          for (int i = 0; i < n_st_diag; ++i) ov[order[k] + (size_t)i * m] = -1.0;
+        }
+        const std::vector<double> y0 = y;
+        std::vector<double> l0(lambda.begin(), lambda.begin() + n_st), s0(s2.begin(), s2.begin() + n_st);
+        for (int k = 0; k < n_st; ++k) {
+          const int l = order[k];
+          if (k != l)
+            for (int i = 0; i < shift2; ++i) y[i + (size_t)k * m] = y0[i + (size_t)l * m];
+        }
+        for (int k = 0; k < n_st; ++k) {
+          const int l = order[k];
+          if (k != l) {
+            lambda[k] = l0[l];
+            s2[k] = s0[l];
           }
         }
       }

@@ -18,6 +18,7 @@ ERRORS = {
 }
 FP64, FP32, FF = 0, 1, 2
 SIGMA_AUTO, SIGMA_STORED, SIGMA_DIRECT = 0, 1, 2  # qpgpu_set_sigma_mode
+ALGEBRA_FAST, ALGEBRA_FP64 = 0, 1  # qpgpu_davidson_params.algebra
 
 HEADER = os.path.join(os.path.dirname(os.path.dirname(os.path.abspath(__file__))), "include", "qpgpu.h")
 
@@ -39,7 +40,8 @@ class DavidsonParams(C.Structure):
     _fields_ = [("n_states", C.c_int32), ("n_states_diag", C.c_int32), ("davidson_sze_max", C.c_int32),
                 ("s2_eig", C.c_int32), ("threshold", C.c_double), ("precision", C.c_int32),
                 ("defect_every", C.c_int32), ("preconditioner", C.c_int32), ("max_iter", C.c_int32),
-                ("collect_every", C.c_int32), ("collect_max", C.c_int32)]
+                ("collect_every", C.c_int32), ("collect_max", C.c_int32), ("state_following", C.c_int32),
+                ("algebra", C.c_int32)]
 
 
 class DavidsonTrace(C.Structure):
@@ -107,6 +109,8 @@ def load():
         "qpgpu_mlp_train": (C.c_int, [vp, C.c_int, C.c_int, C.c_float, C.c_uint64, C.POINTER(C.c_float)]),
         "qpgpu_diag": (C.c_int, [vp, vp, vp]),
         "qpgpu_connected_pairs": (C.c_int, [vp, C.POINTER(C.c_int64), vp, vp, vp, vp, vp, vp, C.c_int64]),
+        "qpgpu_connected_pairs_rows": (C.c_int, [vp, vp, C.c_int64, C.POINTER(C.c_int64), vp, vp, vp, vp, vp, vp,
+                                                 C.c_int64]),
     }
     optional = {}
     sig["qpgpu_davidson_hs2"] = (C.c_int, [vp, vp, C.c_int64, vp, vp, C.POINTER(DavidsonParams),

@@ -508,7 +508,7 @@ struct qpgpu_batch {
   BProb* d = nullptr;
   int64_t total_items = 0;
   unsigned long long* d_counter = nullptr;
-  int sm_count = 152;
+  int sm_count = 0;  // multiprocessors of the problems' device (set at create)
   int tuned_warps = 0, tuned_bps = 0;  // launch shape of the persistent sigma
   double tune_ms = 0.0;
 };
@@ -677,8 +677,7 @@ int qpgpu_batch_create(qpgpu_ctx* const* ctxs, int n, qpgpu_batch** out) {
   qpgpu_batch* B = new qpgpu_batch();
   B->ctx.assign(ctxs, ctxs + n);
   B->np = n;
-  cudaDeviceProp prop;
-  if (cudaGetDeviceProperties(&prop, ctxs[0]->device) == cudaSuccess) B->sm_count = prop.multiProcessorCount;
+  B->sm_count = ctxs[0]->n_sm;
   if (cudaStreamCreateWithFlags(&B->st, cudaStreamNonBlocking) != cudaSuccess ||
       cudaMalloc((void**)&B->d_counter, sizeof(unsigned long long)) != cudaSuccess ||
       cudaMalloc((void**)&B->d, n * sizeof(BProb)) != cudaSuccess) {

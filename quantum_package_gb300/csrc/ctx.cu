@@ -1,4 +1,5 @@
 // C-ABI entry points: context, integral tables, determinant set, sigma.
+#include <algorithm>
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
@@ -73,7 +74,71 @@ __global__ void k_eref(DevTables t, double* out) {
   *out = e;
 }
 
-// connected-pair export (debug): class, phase, excitation of each stored pair
+// connected-pair export (debug): class, phase and excitation of stored pair e
+// (row k) into record o, with the get_mono/double_excitation_spin routines
+// (slater_rules.irp.f:2783-2987)
+struct PairOut {
+  int32_t* I;
+  int32_t* J;
+  int8_t* cls;
+  int8_t* phase;
+  int16_t* exc;
+  double* hij;
+};
+
+template <int NINT>
+__device__ void export_pair(const DevTables& t, const u64* alpha, const u64* beta, const int* rows, const int* cols,
+                            const int* order, const int* colidx, const double* val, int k, int64_t e, int64_t o,
+                            const PairOut& out) {
+  const int jp = colidx[e];
+  u64 di[2 * NINT], dj[2 * NINT];
+  for (int w = 0; w < NINT; ++w) {
+    di[w] = alpha[(int64_t)rows[k] * NINT + w];
+    di[NINT + w] = beta[(int64_t)cols[k] * NINT + w];
+    dj[w] = alpha[(int64_t)rows[jp] * NINT + w];
+    dj[NINT + w] = beta[(int64_t)cols[jp] * NINT + w];
+  }
+  int da = 0, db = 0;
+  for (int w = 0; w < NINT; ++w) {
+    da += popc64(di[w] ^ dj[w]);
+    db += popc64(di[NINT + w] ^ dj[NINT + w]);
+  }
+  int c, neg = 0, x4[4] = {0, 0, 0, 0};
+  double s2;
+  if (db == 0) {
+    c = (da == 2) ? 1 : 3;
+    if (c == 1) h_mono_spin<NINT>(t, di, dj, 1, x4, &neg);
+    else h_double_spin<NINT>(t, di, dj, x4, &neg);
+  } else if (da == 0) {
+    c = (db == 2) ? 2 : 4;
+    if (c == 2) h_mono_spin<NINT>(t, di, dj, 2, x4, &neg);
+    else h_double_spin<NINT>(t, di + NINT, dj + NINT, x4, &neg);
+  } else {
+    c = 5;
+    h_double_ab<NINT>(t, di, dj, &s2, x4, &neg);
+  }
+  out.I[o] = order[k];
+  out.J[o] = order[jp];
+  out.cls[o] = (int8_t)c;
+  out.phase[o] = neg ? -1 : 1;
+  for (int q = 0; q < 4; ++q) out.exc[4 * o + q] = (int16_t)x4[q];
+  out.hij[o] = val[e];
+}
+
+// pairs of selected rows: block b exports the pairs of bilinear row rsel[b]
+// into records starting at obeg[b]
+template <int NINT>
+__global__ void k_export_rows(DevTables t, const u64* alpha, const u64* beta, const int* rows, const int* cols,
+                              const int* order, const int64_t* rowptr, const int* colidx, const double* val,
+                              const int* rsel, const int64_t* obeg, int nsel, PairOut out) {
+  for (int b = blockIdx.x; b < nsel; b += gridDim.x) {
+    const int k = rsel[b];
+    const int64_t rb = rowptr[k], re = rowptr[k + 1];
+    for (int64_t e = rb + threadIdx.x; e < re; e += blockDim.x)
+      export_pair<NINT>(t, alpha, beta, rows, cols, order, colidx, val, k, e, obeg[b] + (e - rb), out);
+  }
+}
+
 template <int NINT>
 __global__ void k_export_pairs(DevTables t, const u64* alpha, const u64* beta, const int* rows, const int* cols,
                                const int* order, const int64_t* rowptr, const int* colidx, const double* val,
@@ -85,39 +150,8 @@ __global__ void k_export_pairs(DevTables t, const u64* alpha, const u64* beta, c
       const int64_t mid = (lo + hi) >> 1;
       if (rowptr[mid] <= e) lo = mid; else hi = mid;
     }
-    const int k = (int)lo, jp = colidx[e];
-    u64 di[2 * NINT], dj[2 * NINT];
-    for (int w = 0; w < NINT; ++w) {
-      di[w] = alpha[(int64_t)rows[k] * NINT + w];
-      di[NINT + w] = beta[(int64_t)cols[k] * NINT + w];
-      dj[w] = alpha[(int64_t)rows[jp] * NINT + w];
-      dj[NINT + w] = beta[(int64_t)cols[jp] * NINT + w];
-    }
-    int da = 0, db = 0;
-    for (int w = 0; w < NINT; ++w) {
-      da += popc64(di[w] ^ dj[w]);
-      db += popc64(di[NINT + w] ^ dj[NINT + w]);
-    }
-    int c, neg = 0, x4[4] = {0, 0, 0, 0};
-    double s2;
-    if (db == 0) {
-      c = (da == 2) ? 1 : 3;
-      if (c == 1) h_mono_spin<NINT>(t, di, dj, 1, x4, &neg);
-      else h_double_spin<NINT>(t, di, dj, x4, &neg);
-    } else if (da == 0) {
-      c = (db == 2) ? 2 : 4;
-      if (c == 2) h_mono_spin<NINT>(t, di, dj, 2, x4, &neg);
-      else h_double_spin<NINT>(t, di + NINT, dj + NINT, x4, &neg);
-    } else {
-      c = 5;
-      h_double_ab<NINT>(t, di, dj, &s2, x4, &neg);
-    }
-    I[e] = order[k];
-    J[e] = order[jp];
-    cls[e] = (int8_t)c;
-    phase[e] = neg ? -1 : 1;
-    for (int q = 0; q < 4; ++q) exc[4 * e + q] = (int16_t)x4[q];
-    hij[e] = val[e];
+    export_pair<NINT>(t, alpha, beta, rows, cols, order, colidx, val, (int)lo, e, e,
+                      PairOut{I, J, cls, phase, exc, hij});
   }
 }
 
@@ -161,6 +195,13 @@ void qp_report_marks(qpgpu_ctx* c) {
   c->marks.clear();
 }
 
+int qp_numeric_flag(qpgpu_ctx* c, cudaStream_t st, int** flag) {
+  if (!c->d_flag) QP_CUDA(c, cudaMalloc((void**)&c->d_flag, 64));
+  QP_CUDA(c, cudaMemsetAsync(c->d_flag, 0, sizeof(int), st));
+  *flag = c->d_flag;
+  return 0;
+}
+
 namespace {
 
 struct Lock {
@@ -195,7 +236,9 @@ int qpgpu_create(int n_mo, int n_alpha, int n_beta, int n_int, qpgpu_ctx** out) 
   }
   if (cudaDeviceGetAttribute(&c->n_sm, cudaDevAttrMultiProcessorCount, c->device) != cudaSuccess || c->n_sm < 1) {
     cudaGetLastError();
-    c->n_sm = 152;
+    cudaStreamDestroy(c->stream);
+    delete c;
+    return QPGPU_ERR_CUDA;
   }
   *out = c;
   return QPGPU_OK;
@@ -215,6 +258,7 @@ int qpgpu_destroy(qpgpu_ctx* c) {
     dev_free(c->d_stage);
     dev_free(c->d_ffu);
     dev_free(c->d_direct_ut);
+    dev_free(c->d_flag);
     cudaStreamDestroy(c->stream);
   }
   delete c;
@@ -388,15 +432,15 @@ int qpgpu_sigma_bilinear(qpgpu_ctx* c, double* v_t, double* s_t, const double* u
   return qp_sigma_launch(c, &c->items, v_t, s_t, u_t, u_t32, n_st, precision, st, 0, (int)c->N, 0, 1);
 }
 
-int qpgpu_h_s2_u0_device(qpgpu_ctx* c, double* v0, double* s0, const double* u0, int n_st, int64_t ld,
-                         int precision, void* stream) {
-  int rc = check_ctx(c, true, true);
-  if (rc) return rc;
-  if (!v0 || !s0 || !u0 || n_st < 1 || ld < c->N || (precision != QPGPU_FP64 && precision != QPGPU_FP32))
-    return qpgpu_fail(c, QPGPU_ERR_ARG, "bad h_s2_u0 arguments");
-  Lock l(c->mu);
+}  // extern "C"
+
+namespace {
+// qpgpu_h_s2_u0_device with an optional device flag that the input conversion
+// sets when u0 holds a NaN or an infinity (called with the context locked)
+int h_s2_u0_dev(qpgpu_ctx* c, double* v0, double* s0, const double* u0, int n_st, int64_t ld, int precision,
+                cudaStream_t st, int* bad) {
   const int64_t N = c->N;
-  cudaStream_t st = stream ? (cudaStream_t)stream : c->stream;
+  int rc = 0;
   const int nb = n_st < 8 ? n_st : 8;
   rc = ensure_work(c, (size_t)N * nb * (3 * sizeof(double) + sizeof(float)) + 1024);
   if (rc) return rc;
@@ -406,7 +450,8 @@ int qpgpu_h_s2_u0_device(qpgpu_ctx* c, double* v0, double* s0, const double* u0,
   float* ut32 = (float*)(stt + (size_t)N * nb);
   for (int s0i = 0; s0i < n_st; s0i += 8) {
     const int m = (n_st - s0i) < 8 ? (n_st - s0i) : 8;
-    qp_to_bilinear(u0 + (int64_t)s0i * ld, ld, c->d_order, ut, precision == QPGPU_FP32 ? ut32 : nullptr, m, N, st);
+    qp_to_bilinear(u0 + (int64_t)s0i * ld, ld, c->d_order, ut, precision == QPGPU_FP32 ? ut32 : nullptr, m, N, st,
+                   bad);
     rc = qp_sigma_launch(c, &c->items, vt, stt, ut, ut32, m, precision, st, 0, (int)N, 0, 1);
     if (rc) return rc;
     qp_from_bilinear(vt, ld, c->d_order, v0 + (int64_t)s0i * ld, m, N, st);
@@ -415,6 +460,19 @@ int qpgpu_h_s2_u0_device(qpgpu_ctx* c, double* v0, double* s0, const double* u0,
   QP_CUDA(c, cudaGetLastError());
   return QPGPU_OK;
 }
+}  // namespace
+
+extern "C" {
+
+int qpgpu_h_s2_u0_device(qpgpu_ctx* c, double* v0, double* s0, const double* u0, int n_st, int64_t ld,
+                         int precision, void* stream) {
+  int rc = check_ctx(c, true, true);
+  if (rc) return rc;
+  if (!v0 || !s0 || !u0 || n_st < 1 || ld < c->N || (precision != QPGPU_FP64 && precision != QPGPU_FP32))
+    return qpgpu_fail(c, QPGPU_ERR_ARG, "bad h_s2_u0 arguments");
+  Lock l(c->mu);
+  return h_s2_u0_dev(c, v0, s0, u0, n_st, ld, precision, stream ? (cudaStream_t)stream : c->stream, nullptr);
+}
 
 int qpgpu_h_s2_u0(qpgpu_ctx* c, double* v0, double* s0, const double* u0, int n_st, int64_t ld) {
   int rc = check_ctx(c, true, true);
@@ -422,35 +480,39 @@ int qpgpu_h_s2_u0(qpgpu_ctx* c, double* v0, double* s0, const double* u0, int n_
   if (!v0 || !s0 || !u0 || n_st < 1 || ld < c->N) return qpgpu_fail(c, QPGPU_ERR_ARG, "bad h_s2_u0 arguments");
   const int64_t N = c->N;
   const size_t cols = (size_t)N * n_st;
-  {
-    Lock l(c->mu);
-    if (c->stage_bytes < 3 * cols * sizeof(double)) {
-      dev_free(c->d_stage);
-      c->d_stage = nullptr;
-      c->stage_bytes = 0;
-      QP_CUDA(c, cudaMalloc((void**)&c->d_stage, 3 * cols * sizeof(double)));
-      c->stage_bytes = 3 * cols * sizeof(double);
-    }
+  Lock l(c->mu);
+  if (c->stage_bytes < 3 * cols * sizeof(double)) {
+    dev_free(c->d_stage);
+    c->d_stage = nullptr;
+    c->stage_bytes = 0;
+    QP_CUDA(c, cudaMalloc((void**)&c->d_stage, 3 * cols * sizeof(double)));
+    c->stage_bytes = 3 * cols * sizeof(double);
   }
   double *du = c->d_stage, *dv = du + cols, *ds = du + 2 * cols;
   cudaStream_t st = c->stream;
-  rc = 0;
+  int* bad = nullptr;
+  rc = qp_numeric_flag(c, st, &bad);
+  if (rc) return rc;
+  int hbad = 0;
   if (cudaMemcpy2DAsync(du, N * sizeof(double), u0, ld * sizeof(double), N * sizeof(double), n_st,
                         cudaMemcpyHostToDevice, st) != cudaSuccess)
     rc = qpgpu_fail(c, QPGPU_ERR_CUDA, "copy of u_0 failed");
-  if (!rc) rc = qpgpu_h_s2_u0_device(c, dv, ds, du, n_st, N, QPGPU_FP64, st);
+  if (!rc) rc = h_s2_u0_dev(c, dv, ds, du, n_st, N, QPGPU_FP64, st, bad);
   if (!rc && (cudaMemcpy2DAsync(v0, ld * sizeof(double), dv, N * sizeof(double), N * sizeof(double), n_st,
                                 cudaMemcpyDeviceToHost, st) != cudaSuccess ||
               cudaMemcpy2DAsync(s0, ld * sizeof(double), ds, N * sizeof(double), N * sizeof(double), n_st,
-                                cudaMemcpyDeviceToHost, st) != cudaSuccess))
+                                cudaMemcpyDeviceToHost, st) != cudaSuccess ||
+              cudaMemcpyAsync(&hbad, bad, sizeof(int), cudaMemcpyDeviceToHost, st) != cudaSuccess))
     rc = qpgpu_fail(c, QPGPU_ERR_CUDA, "copy of v_0/s_0 failed");
   cudaError_t e = cudaStreamSynchronize(st);
   if (!rc && e != cudaSuccess) rc = qpgpu_fail(c, QPGPU_ERR_CUDA, cudaGetErrorString(e));
+  if (!rc && hbad) rc = qpgpu_fail(c, QPGPU_ERR_NUMERIC, "u_0 holds a NaN or an infinity");
   return rc;
 }
 
 namespace {
-constexpr int DOT_CTA = 256, DOT_GRID = 2 * 152;
+constexpr int DOT_CTA = 256;
+inline int dot_grid(const qpgpu_ctx* c) { return 2 * c->n_sm; }  // two CTAs per SM
 // per-CTA partial sums of u.u and u.v for each column (fixed summation order)
 __global__ void k_col_dots(const double* u, const double* v, int64_t N, int n_st, double* partial) {
   __shared__ double red[2][DOT_CTA / 32];
@@ -489,38 +551,42 @@ int qpgpu_u0_h_u0(qpgpu_ctx* c, double* e_0, const double* u0, int n_st, int64_t
   if (!e_0 || !u0 || n_st < 1 || ld < c->N) return qpgpu_fail(c, QPGPU_ERR_ARG, "bad u_0_H_u_0 arguments");
   const int64_t N = c->N;
   const size_t cols = (size_t)N * n_st;
-  {
-    Lock l(c->mu);
-    if (c->stage_bytes < 3 * cols * sizeof(double)) {
-      dev_free(c->d_stage);
-      c->d_stage = nullptr;
-      c->stage_bytes = 0;
-      QP_CUDA(c, cudaMalloc((void**)&c->d_stage, 3 * cols * sizeof(double)));
-      c->stage_bytes = 3 * cols * sizeof(double);
-    }
+  Lock l(c->mu);
+  if (c->stage_bytes < 3 * cols * sizeof(double)) {
+    dev_free(c->d_stage);
+    c->d_stage = nullptr;
+    c->stage_bytes = 0;
+    QP_CUDA(c, cudaMalloc((void**)&c->d_stage, 3 * cols * sizeof(double)));
+    c->stage_bytes = 3 * cols * sizeof(double);
   }
   double *du = c->d_stage, *dv = du + cols, *ds = du + 2 * cols;
   cudaStream_t st = c->stream;
+  const int grid = dot_grid(c);
   double* dpart = nullptr;
-  QP_CUDA(c, cudaMalloc((void**)&dpart, (size_t)DOT_GRID * n_st * 2 * sizeof(double)));
-  std::vector<double> part((size_t)DOT_GRID * n_st * 2);
-  if (cudaMemcpy2DAsync(du, N * sizeof(double), u0, ld * sizeof(double), N * sizeof(double), n_st,
-                        cudaMemcpyHostToDevice, st) != cudaSuccess)
+  QP_CUDA(c, cudaMalloc((void**)&dpart, (size_t)grid * n_st * 2 * sizeof(double)));
+  std::vector<double> part((size_t)grid * n_st * 2);
+  int* bad = nullptr;
+  int hbad = 0;
+  rc = qp_numeric_flag(c, st, &bad);
+  if (!rc && cudaMemcpy2DAsync(du, N * sizeof(double), u0, ld * sizeof(double), N * sizeof(double), n_st,
+                               cudaMemcpyHostToDevice, st) != cudaSuccess)
     rc = qpgpu_fail(c, QPGPU_ERR_CUDA, "copy of u_0 failed");
-  if (!rc) rc = qpgpu_h_s2_u0_device(c, dv, ds, du, n_st, N, QPGPU_FP64, st);
+  if (!rc) rc = h_s2_u0_dev(c, dv, ds, du, n_st, N, QPGPU_FP64, st, bad);
   if (!rc) {
-    k_col_dots<<<DOT_GRID, DOT_CTA, 0, st>>>(du, dv, N, n_st, dpart);
+    k_col_dots<<<grid, DOT_CTA, 0, st>>>(du, dv, N, n_st, dpart);
     if (cudaMemcpyAsync(part.data(), dpart, part.size() * sizeof(double), cudaMemcpyDeviceToHost, st) !=
-        cudaSuccess)
+            cudaSuccess ||
+        cudaMemcpyAsync(&hbad, bad, sizeof(int), cudaMemcpyDeviceToHost, st) != cudaSuccess)
       rc = qpgpu_fail(c, QPGPU_ERR_CUDA, "copy of the dot products failed");
   }
   const cudaError_t e = cudaStreamSynchronize(st);
   cudaFree(dpart);
   if (!rc && e != cudaSuccess) rc = qpgpu_fail(c, QPGPU_ERR_CUDA, cudaGetErrorString(e));
+  if (!rc && hbad) rc = qpgpu_fail(c, QPGPU_ERR_NUMERIC, "u_0 holds a NaN or an infinity");
   if (rc) return rc;
   for (int i = 0; i < n_st; ++i) {
     double uu = 0.0, uv = 0.0;
-    for (int q = 0; q < DOT_GRID; ++q) {
+    for (int q = 0; q < grid; ++q) {
       uu += part[((size_t)q * n_st + i) * 2];
       uv += part[((size_t)q * n_st + i) * 2 + 1];
     }
@@ -546,14 +612,21 @@ int qpgpu_h_s2_u0_work(qpgpu_ctx* c, double* v_t, double* s_t, const double* u_t
   if (cudaMemcpyAsync(buf, u_t, cnt * sizeof(double), cudaMemcpyHostToDevice, st) != cudaSuccess)
     rc = qpgpu_fail(c, QPGPU_ERR_CUDA, "copy of u_t failed");
   const int first = istart - 1 + ishift;
+  int* bad = nullptr;
+  int hbad = 0;
+  if (!rc) rc = qp_numeric_flag(c, st, &bad);
+  if (!rc) qp_flag_nonfinite(buf, (int64_t)cnt, bad, st);
   if (!rc) rc = qp_sigma_launch(c, &c->items, buf + cnt, buf + 2 * cnt, buf, nullptr, n_st, QPGPU_FP64, st, first,
                                 iend, first, istep);
+  if (!rc && cudaMemcpyAsync(&hbad, bad, sizeof(int), cudaMemcpyDeviceToHost, st) != cudaSuccess)
+    rc = qpgpu_fail(c, QPGPU_ERR_CUDA, "copy of the NaN flag failed");
   if (!rc && (cudaMemcpyAsync(hv.data(), buf + cnt, cnt * sizeof(double), cudaMemcpyDeviceToHost, st) != cudaSuccess ||
               cudaMemcpyAsync(hs.data(), buf + 2 * cnt, cnt * sizeof(double), cudaMemcpyDeviceToHost, st) != cudaSuccess))
     rc = qpgpu_fail(c, QPGPU_ERR_CUDA, "copy of v_t/s_t failed");
   cudaError_t e = cudaStreamSynchronize(st);
   cudaFree(buf);
   if (!rc && e != cudaSuccess) rc = qpgpu_fail(c, QPGPU_ERR_CUDA, cudaGetErrorString(e));
+  if (!rc && hbad) rc = qpgpu_fail(c, QPGPU_ERR_NUMERIC, "u_t holds a NaN or an infinity");
   if (rc) return rc;
   for (int64_t k = first; k < iend; k += istep)
     for (int q = 0; q < n_st; ++q) {
@@ -631,6 +704,74 @@ int qpgpu_connected_pairs(qpgpu_ctx* c, int64_t* n_pairs, int32_t* I, int32_t* J
   cudaError_t e = cudaStreamSynchronize(st);
   cudaFree(buf);
   if (rc || e != cudaSuccess) return qpgpu_fail(c, QPGPU_ERR_CUDA, "connected_pairs copy failed");
+  return QPGPU_OK;
+}
+
+int qpgpu_connected_pairs_rows(qpgpu_ctx* c, const int32_t* rows, int64_t n_rows, int64_t* n_pairs, int32_t* I,
+                               int32_t* J, int8_t* cls, int8_t* phase, int16_t* exc, double* hij, int64_t cap) {
+  int rc = check_ctx(c, true, true);
+  if (rc) return rc;
+  if (!n_pairs || n_rows < 0 || (n_rows > 0 && !rows)) return qpgpu_fail(c, QPGPU_ERR_ARG, "bad row list");
+  Lock l(c->mu);
+  if (c->direct) return qpgpu_fail(c, QPGPU_ERR_STATE, "pairs are not stored (direct sigma)");
+  const int64_t N = c->N;
+  for (int64_t i = 0; i < n_rows; ++i)
+    if (rows[i] < 0 || rows[i] >= N) return qpgpu_fail(c, QPGPU_ERR_ARG, "row index outside 0..N_det-1");
+  cudaStream_t st = c->stream;
+  std::vector<int> order(N);
+  std::vector<int64_t> rowptr(N + 1);
+  QP_CUDA(c, cudaMemcpyAsync(order.data(), c->d_order, N * sizeof(int), cudaMemcpyDeviceToHost, st));
+  QP_CUDA(c, cudaMemcpyAsync(rowptr.data(), c->d_rowptr, (N + 1) * sizeof(int64_t), cudaMemcpyDeviceToHost, st));
+  QP_CUDA(c, cudaStreamSynchronize(st));
+  std::vector<int> inv(N);
+  for (int64_t k = 0; k < N; ++k) inv[order[k]] = (int)k;
+  std::vector<int> sel((size_t)n_rows);
+  for (int64_t i = 0; i < n_rows; ++i) sel[i] = inv[rows[i]];
+  std::sort(sel.begin(), sel.end());
+  sel.erase(std::unique(sel.begin(), sel.end()), sel.end());
+  std::vector<int64_t> beg(sel.size() + 1, 0);
+  for (size_t b = 0; b < sel.size(); ++b) beg[b + 1] = beg[b] + (rowptr[sel[b] + 1] - rowptr[sel[b]]);
+  const int64_t P = beg.back();
+  *n_pairs = P;
+  if (cap <= 0 || sel.empty()) return QPGPU_OK;
+  if (cap < P || !I || !J || !cls || !phase || !exc || !hij)
+    return qpgpu_fail(c, QPGPU_ERR_ARG, "connected_pairs_rows: cap below n_pairs or null output");
+  char* buf = nullptr;
+  const size_t bytes = P * (4 + 4 + 1 + 1 + 8 + 8) + sel.size() * (4 + 8) + 128;
+  QP_CUDA(c, cudaMalloc((void**)&buf, bytes));
+  double* dh = (double*)buf;
+  int64_t* dbeg = (int64_t*)(dh + P);
+  int32_t* dI = (int32_t*)(dbeg + sel.size());
+  int32_t* dJ = dI + P;
+  int32_t* dsel = dJ + P;
+  int16_t* dx = (int16_t*)(dsel + sel.size());
+  int8_t* dc = (int8_t*)(dx + 4 * P);
+  int8_t* dp = dc + P;
+  rc = 0;
+  if (cudaMemcpyAsync(dsel, sel.data(), sel.size() * 4, cudaMemcpyHostToDevice, st) != cudaSuccess ||
+      cudaMemcpyAsync(dbeg, beg.data(), sel.size() * 8, cudaMemcpyHostToDevice, st) != cudaSuccess)
+    rc = -1;
+  const PairOut out{dI, dJ, dc, dp, dx, dh};
+  const unsigned grid = (unsigned)std::min<size_t>(sel.size(), 65535);
+  if (!rc) {
+    if (c->nint == 1)
+      k_export_rows<1><<<grid, 256, 0, st>>>(c->tab, c->d_alpha, c->d_beta, c->d_rows, c->d_cols, c->d_order,
+                                             c->d_rowptr, c->d_colidx, c->d_val64, dsel, dbeg, (int)sel.size(), out);
+    else
+      k_export_rows<2><<<grid, 256, 0, st>>>(c->tab, c->d_alpha, c->d_beta, c->d_rows, c->d_cols, c->d_order,
+                                             c->d_rowptr, c->d_colidx, c->d_val64, dsel, dbeg, (int)sel.size(), out);
+    if (cudaGetLastError() != cudaSuccess) rc = -1;
+  }
+  if (!rc && (cudaMemcpyAsync(I, dI, P * 4, cudaMemcpyDeviceToHost, st) != cudaSuccess ||
+              cudaMemcpyAsync(J, dJ, P * 4, cudaMemcpyDeviceToHost, st) != cudaSuccess ||
+              cudaMemcpyAsync(hij, dh, P * 8, cudaMemcpyDeviceToHost, st) != cudaSuccess ||
+              cudaMemcpyAsync(exc, dx, P * 8, cudaMemcpyDeviceToHost, st) != cudaSuccess ||
+              cudaMemcpyAsync(cls, dc, P, cudaMemcpyDeviceToHost, st) != cudaSuccess ||
+              cudaMemcpyAsync(phase, dp, P, cudaMemcpyDeviceToHost, st) != cudaSuccess))
+    rc = -1;
+  cudaError_t e = cudaStreamSynchronize(st);
+  cudaFree(buf);
+  if (rc || e != cudaSuccess) return qpgpu_fail(c, QPGPU_ERR_CUDA, "connected_pairs_rows export failed");
   return QPGPU_OK;
 }
 

@@ -1058,7 +1058,7 @@ int gram(Dav& d, const double* A, int m, const double* B0, const double* B1, dou
 // float-float copy of one block (X1 = nullptr) or of [X0 X1]
 void split_block(Dav& d, const double* X0, const double* X1, float2* out, const int* skip = nullptr) {
   const int nx = X1 ? 2 : 1;
-  k_split_block<<<std::min<unsigned>(gsz(d.N * d.nsd), 152 * 8), DBLK, 0, d.st>>>(X0, X1, d.nsd, nx, d.N, out, skip);
+  k_split_block<<<std::min<unsigned>(gsz(d.N * d.nsd), d.c->n_sm * 8), DBLK, 0, d.st>>>(X0, X1, d.nsd, nx, d.N, out, skip);
 }
 
 // out (m x nbc) = A^T B on split operands: A = m columns of consecutive split
@@ -1122,7 +1122,7 @@ void lincomb(Dav& d, int m, const double* C, const double* A0, double* O0, const
     L.n = 3;
   }
   const int nb = m / d.nsd;
-  const unsigned grid = std::min<unsigned>(gsz(d.N), 152 * 8);
+  const unsigned grid = std::min<unsigned>(gsz(d.N), d.c->n_sm * 8);
   switch (d.nsd) {
 #define QP_LC_CASE(NS) \
   case NS:             \
@@ -1159,7 +1159,7 @@ void lincomb_ff(Dav& d, int m, const double* C, const double* A0, double* O0, co
     L.n = 3;
   }
   const int nb = m / d.nsd;
-  const unsigned grid = std::min<unsigned>(gsz(d.N), 152 * 8);
+  const unsigned grid = std::min<unsigned>(gsz(d.N), d.c->n_sm * 8);
   switch (d.nsd) {
 #define QP_LCF_CASE(NS) \
   case NS:              \
@@ -1189,7 +1189,7 @@ void lincomb32(Dav& d, int m, const double* C, const double* A0, double* O0, con
   L.out[2] = O2;
   L.n = 3;
   const int nb = m / d.nsd;
-  const unsigned grid = std::min<unsigned>(gsz(d.N), 152 * 8);
+  const unsigned grid = std::min<unsigned>(gsz(d.N), d.c->n_sm * 8);
   switch (d.nsd) {
 #define QP_LC32_CASE(NS) \
   case NS:               \
@@ -1306,12 +1306,17 @@ extern "C" int qpgpu_davidson_hs2(qpgpu_ctx* c, double* u_in, int64_t dim_in, do
   if (nst < 1 || nsd < nst || nsd > MAXS || dim_in < N || prm->davidson_sze_max < 1 ||
       (prm->precision != QPGPU_FP64 && prm->precision != QPGPU_FP32 && prm->precision != QPGPU_FF))
     return qpgpu_fail(c, QPGPU_ERR_ARG, "bad Davidson parameters (1 <= n_states <= n_states_diag <= 8)");
+  if (prm->algebra != QPGPU_ALGEBRA_FAST && prm->algebra != QPGPU_ALGEBRA_FP64)
+    return qpgpu_fail(c, QPGPU_ERR_ARG, "algebra must be QPGPU_ALGEBRA_FAST or QPGPU_ALGEBRA_FP64");
   if (prm->preconditioner < 0 || prm->preconditioner > 2)
     return qpgpu_fail(c, QPGPU_ERR_ARG, "preconditioner must be 0 (diagonal), 1 (learned) or 2 (learned, extra direction)");
   if ((int64_t)nsd * 3 > N) return qpgpu_fail(c, QPGPU_ERR_ARG, "N_st_diag*3 > sze (diagonalization_hs2.irp.f:110)");
   int itermax = std::max(3, (int)std::min<int64_t>(prm->davidson_sze_max, N / nsd));
   while (itermax * nsd > MAXM) --itermax;
   const bool mixed = prm->precision == QPGPU_FP32 || prm->precision == QPGPU_FF;
+  // tall-skinny algebra of the mixed modes on the FP32 pipes (float-float /
+  // FP32), or in FP64 like the plain loop (algebra = QPGPU_ALGEBRA_FP64)
+  const bool ffalg = mixed && prm->algebra == QPGPU_ALGEBRA_FAST;
   const int restart_prec = prm->precision == QPGPU_FF ? QPGPU_FF : QPGPU_FP64;  // defect-correction sigma
   if (mixed && prm->defect_every > 0) itermax = std::max(3, std::min(itermax, prm->defect_every + 1));
   const int max_sigma = prm->max_iter > 0 ? prm->max_iter : 1000;
@@ -1324,7 +1329,7 @@ extern "C" int qpgpu_davidson_hs2(qpgpu_ctx* c, double* u_in, int64_t dim_in, do
   d.nsd = nsd;
   d.nst = nst;
   d.itermax = itermax;
-  d.ncta = 2 * 152;
+  d.ncta = 2 * c->n_sm;  // two CTAs per SM
   d.rows_per_cta = (N + d.ncta - 1) / d.ncta;
   const size_t blkn = (size_t)N * nsd;
   if (dev_alloc(&d.U, blkn * itermax) != cudaSuccess || dev_alloc(&d.W, blkn * itermax) != cudaSuccess ||
@@ -1335,7 +1340,7 @@ extern "C" int qpgpu_davidson_hs2(qpgpu_ctx* c, double* u_in, int64_t dim_in, do
     return qpgpu_fail(c, QPGPU_ERR_NOMEM, "Davidson work arrays do not fit on the device");
   }
   d.sUf = (int64_t)blkn;
-  if (mixed && (dev_alloc(&d.Uf, blkn * itermax) != cudaSuccess || dev_alloc(&d.Bf, blkn * 2) != cudaSuccess)) {
+  if (ffalg && (dev_alloc(&d.Uf, blkn * itermax) != cudaSuccess || dev_alloc(&d.Bf, blkn * 2) != cudaSuccess)) {
     cudaGetLastError();
     return qpgpu_fail(c, QPGPU_ERR_NOMEM, "mixed-precision work arrays do not fit on the device");
   }
@@ -1381,9 +1386,18 @@ extern "C" int qpgpu_davidson_hs2(qpgpu_ctx* c, double* u_in, int64_t dim_in, do
     QP_CUDA(c, cudaMalloc((void**)&hstage, blkn * sizeof(double)));
     QP_CUDA(c, cudaMemcpy2DAsync(hstage, N * sizeof(double), u_in, dim_in * sizeof(double), N * sizeof(double), nsd,
                                  cudaMemcpyHostToDevice, st));
-    qp_to_bilinear(hstage, N, c->d_order, d.U, nullptr, nsd, N, st);
+    int* bad = nullptr;
+    int hbad = 0;
+    const int rcf = qp_numeric_flag(c, st, &bad);
+    if (rcf) return rcf;
+    qp_to_bilinear(hstage, N, c->d_order, d.U, nullptr, nsd, N, st, bad);
+    QP_CUDA(c, cudaMemcpyAsync(&hbad, bad, sizeof(int), cudaMemcpyDeviceToHost, st));
     QP_CUDA(c, cudaStreamSynchronize(st));
     cudaFree(hstage);
+    if (hbad) {
+      cudaEventDestroy(ev0);
+      return qpgpu_fail(c, QPGPU_ERR_NUMERIC, "the guess vectors hold a NaN or an infinity");
+    }
   }
   const double Sz = 0.5 * (c->na - c->nb);
   const double sz2sz = Sz * (Sz - 1.0), expected_s2 = Sz * (Sz + 1.0);
@@ -1415,7 +1429,7 @@ extern "C" int qpgpu_davidson_hs2(qpgpu_ctx* c, double* u_in, int64_t dim_in, do
       const int b = iter - 1;
       const int shift = nsd * b;
       shift2 = nsd * iter;
-      orthonormalise(d, b, mixed);
+      orthonormalise(d, b, ffalg);
       prof.mark(DavProf::ORTHO);
       // sigma on block b
       const int prec = (mixed && iter > 1) ? QPGPU_FP32 : restart_prec;
@@ -1429,7 +1443,7 @@ extern "C" int qpgpu_davidson_hs2(qpgpu_ctx* c, double* u_in, int64_t dim_in, do
       prof.mark(DavProf::SIGMA);
       // new Gram columns
       // h(:, new) and s(:, new) in one pass over U: X = U^T [W_b S_b]
-      if (mixed) {
+      if (ffalg) {
         split_block(d, d.blk(d.W, b), d.blk(d.S, b), d.Bf);
         gram_ff(d, d.Uf, shift2, d.Bf, 2 * nsd, d.small + OFF_X);
       } else {
@@ -1486,6 +1500,34 @@ extern "C" int qpgpu_davidson_hs2(qpgpu_ctx* c, double* u_in, int64_t dim_in, do
             break;
           }
       }
+      // state following (:328-370): for target k, order[k] is the row i < nst
+      // (the component along the guess / previous Ritz vector i) of largest
+      // |y(i,k)| among the rows not taken by an earlier target; the reference
+      // then takes Ritz vector order[k] as target k (its row index serves as
+      // a column index), with its eigenvalue and S^2
+      if (prm->state_following) {
+        std::vector<double> ov((size_t)shift2 * shift2);
+        for (size_t q = 0; q < ov.size(); ++q) ov[q] = std::fabs(y[q]);
+        std::vector<int> order(nst);
+        for (int k = 0; k < nst; ++k) {
+          double cmax = -1.0;
+          for (int i = 0; i < nst; ++i)
+            if (ov[(size_t)i * shift2 + k] > cmax) {
+              cmax = ov[(size_t)i * shift2 + k];
+              order[k] = i;
+            }
+          for (int i = 0; i < nsd; ++i) ov[(size_t)order[k] * shift2 + i] = -1.0;
+        }
+        const std::vector<double> y0 = y;
+        const std::vector<double> l0(lambda.begin(), lambda.begin() + nst), s0(s2.begin(), s2.begin() + nst);
+        for (int k = 0; k < nst; ++k) {
+          const int l = order[k];
+          if (l == k) continue;
+          for (int i = 0; i < shift2; ++i) y[(size_t)i * shift2 + k] = y0[(size_t)i * shift2 + l];
+          lambda[k] = l0[l];
+          s2[k] = s0[l];
+        }
+      }
       // Ritz vectors into block b+1 (:376-381); coefficients y(0:shift2, 0:nsd)
       std::vector<double> ycoef((size_t)shift2 * nsd);
       for (int i = 0; i < shift2; ++i)
@@ -1493,9 +1535,9 @@ extern "C" int qpgpu_davidson_hs2(qpgpu_ctx* c, double* u_in, int64_t dim_in, do
       double* ydev = d.small + OFF_Y;
       prof.mark(DavProf::HOST);
       QP_CUDA(c, cudaMemcpyAsync(ydev, ycoef.data(), ycoef.size() * sizeof(double), cudaMemcpyHostToDevice, st));
-      if (prec == QPGPU_FP32)  // W, S from the FP32 sigma: Ritz vectors in FP32, they only feed the step
+      if (ffalg && prec == QPGPU_FP32)  // W, S from the FP32 sigma: Ritz vectors in FP32, they only feed the step
         lincomb32(d, shift2, ydev, d.U, d.blk(d.U, iter), d.W, d.blk(d.W, iter), d.S, d.blk(d.S, iter));
-      else if (mixed)  // restart iteration: float-float
+      else if (ffalg)  // restart iteration: float-float
         lincomb_ff(d, shift2, ydev, d.U, d.blk(d.U, iter), d.W, d.blk(d.W, iter), d.S, d.blk(d.S, iter));
       else
         lincomb(d, shift2, ydev, d.U, d.blk(d.U, iter), d.W, d.blk(d.W, iter), d.S, d.blk(d.S, iter));
@@ -1521,11 +1563,11 @@ extern "C" int qpgpu_davidson_hs2(qpgpu_ctx* c, double* u_in, int64_t dim_in, do
       if (mask) {
         k_mlp_features<<<gsz(N), DBLK, 0, st>>>(d.blk(d.U, iter), d.blk(d.W, iter), d.blk(d.S, iter), c->d_hdiag,
                                                 (const float4*)c->d_detfeat, N, sp, d.mlpX);
-        qp_mlp_eval(c->mlp.params, d.mlpX, d.mlpG, N * nst, st);
+        qp_mlp_eval(c->mlp.params, d.mlpX, d.mlpG, N * nst, st, c->n_sm);
         k_step_mlp<<<d.ncta, DBLK, 0, st>>>(d.blk(d.U, iter), d.blk(d.W, iter), d.blk(d.S, iter), c->d_hdiag, d.mlpG,
                                             N, sp, mask, mlp_extra, d.part);
       }
-      else if (mixed)
+      else if (ffalg)
         k_step_mixed<<<d.ncta, DBLK, 0, st>>>(d.blk(d.U, iter), d.blk(d.W, iter), d.blk(d.S, iter), c->d_hdiag, N, sp,
                                               d.part);
       else
@@ -1577,7 +1619,7 @@ extern "C" int qpgpu_davidson_hs2(qpgpu_ctx* c, double* u_in, int64_t dim_in, do
       for (int j = 0; j < nsd; ++j) ycoef[(size_t)i * nsd + j] = y[(size_t)i * shift2 + j];
     double* ydev = d.small + OFF_Y;
     QP_CUDA(c, cudaMemcpyAsync(ydev, ycoef.data(), ycoef.size() * sizeof(double), cudaMemcpyHostToDevice, st));
-    if (mixed)
+    if (ffalg)
       lincomb_ff(d, shift2, ydev, d.U, d.R);
     else
       lincomb(d, shift2, ydev, d.U, d.R);

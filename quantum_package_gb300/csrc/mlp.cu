@@ -183,8 +183,8 @@ __global__ void __launch_bounds__(256) k_mlp_predict(const float* P, const float
 }  // namespace
 
 // y[q] = MLP(X[q]) for n samples (inference of the learned Davidson step)
-void qp_mlp_eval(const float* P, const float* X, float* y, int64_t n, cudaStream_t st) {
-  const int64_t g = std::min<int64_t>(gsz(n), 152 * 8);
+void qp_mlp_eval(const float* P, const float* X, float* y, int64_t n, cudaStream_t st, int n_sm) {
+  const int64_t g = std::min<int64_t>(gsz(n), (int64_t)n_sm * 8);
   k_mlp_predict<<<(unsigned)std::max<int64_t>(g, 1), 256, 0, st>>>(P, X, y, n);
 }
 

@@ -357,7 +357,7 @@ struct MlpState {
 struct qpgpu_ctx {
   std::mutex mu;
   int device = 0;
-  int n_sm = 152;  // streaming multiprocessors of the device
+  int n_sm = 0;  // streaming multiprocessors of the device (read at create)
   cudaStream_t stream = nullptr;
   std::string last_error;
 
@@ -428,6 +428,7 @@ struct qpgpu_ctx {
   bool profile = false;
   std::vector<std::pair<std::string, cudaEvent_t>> marks;
 
+  int* d_flag = nullptr;  // NaN / Inf flag of the host-array entry points
   // scratch for the host-pointer sigma entry points
   double* d_work = nullptr;
   size_t work_bytes = 0;
@@ -471,8 +472,13 @@ int qp_sigma_ff(qpgpu_ctx* c, SigmaItems* it, double* v, double* s, const double
                 int row_lo, int row_hi, int row_first, int row_step);
 // FP32 row length that keeps a row of n_st coefficients in one 32-byte sector
 inline int qp_pad_states(int nst) { return nst <= 1 ? 1 : nst <= 2 ? 2 : nst <= 4 ? 4 : 8; }
+// bad (optional, device int): set to 1 when an input coefficient is not finite
 void qp_to_bilinear(const double* u0, int64_t ld, const int* order, double* ut, float* ut32, int nst, int64_t N,
-                    cudaStream_t st);
+                    cudaStream_t st, int* bad = nullptr);
+void qp_flag_nonfinite(const double* x, int64_t n, int* bad, cudaStream_t st);
+// device flag of the context for the NaN / Inf checks of host-array entry
+// points (allocated on first use), cleared on stream st
+int qp_numeric_flag(qpgpu_ctx* c, cudaStream_t st, int** flag);
 void qp_from_bilinear(const double* vt, int64_t ld, const int* order, double* v0, int nst, int64_t N,
                       cudaStream_t st);
 void qp_to_float(const double* x, float* y, int64_t N, int nst, int ld, cudaStream_t st);
@@ -490,7 +496,7 @@ void qp_report_marks(qpgpu_ctx* c);  // ctx.cu
 // learned preconditioner (mlp.cu)
 int qp_det_features(qpgpu_ctx* c);
 int qp_mlp_append(qpgpu_ctx* c, const float* X, const float* G, const float* W, int64_t n, bool device_src);
-void qp_mlp_eval(const float* P, const float* X, float* y, int64_t n, cudaStream_t st);
+void qp_mlp_eval(const float* P, const float* X, float* y, int64_t n, cudaStream_t st, int n_sm);
 #ifdef __CUDACC__
 __device__ __forceinline__ float qp_gelu(float x) { return 0.5f * x * (1.0f + erff(x * 0.70710678118654752f)); }
 __device__ __forceinline__ float qp_gelu_grad(float x) {

@@ -284,16 +284,23 @@ __global__ void k_fill_items(const int* nit, const int* item0, int* item_row, in
     }
 }
 
+// bad (optional): set to 1 when an input coefficient is NaN or infinite
 template <class T>
 __global__ void k_to_bilinear(const T* u0, int64_t ld, const int* order, double* ut, float* ut32, int nst,
-                              int64_t N) {
+                              int64_t N, int* bad) {
   for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < N * nst; t += (int64_t)gridDim.x * blockDim.x) {
     const int64_t p = t / nst;
     const int st = (int)(t % nst);
     const double x = (double)u0[(int64_t)st * ld + order[p]];
+    if (bad && !isfinite(x)) *bad = 1;
     if (ut) ut[t] = x;
     if (ut32) ut32[t] = (float)x;
   }
+}
+
+__global__ void k_nonfinite(const double* x, int64_t n, int* bad) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+    if (!isfinite(x[i])) *bad = 1;
 }
 
 __global__ void k_from_bilinear(const double* vt, int64_t ld, const int* order, double* v0, int nst, int64_t N) {
@@ -634,8 +641,12 @@ int qp_sigma_launch(qpgpu_ctx* c, SigmaItems* it, double* v, double* s, const do
 }
 
 void qp_to_bilinear(const double* u0, int64_t ld, const int* order, double* ut, float* ut32, int nst, int64_t N,
-                    cudaStream_t st) {
-  k_to_bilinear<double><<<gsz(N * nst, 256), 256, 0, st>>>(u0, ld, order, ut, ut32, nst, N);
+                    cudaStream_t st, int* bad) {
+  k_to_bilinear<double><<<gsz(N * nst, 256), 256, 0, st>>>(u0, ld, order, ut, ut32, nst, N, bad);
+}
+
+void qp_flag_nonfinite(const double* x, int64_t n, int* bad, cudaStream_t st) {
+  k_nonfinite<<<gsz(n, 256), 256, 0, st>>>(x, n, bad);
 }
 
 void qp_from_bilinear(const double* vt, int64_t ld, const int* order, double* v0, int nst, int64_t N,

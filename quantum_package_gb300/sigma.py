@@ -165,10 +165,29 @@ class Wavefunction:
         o = np.lexsort((J, I))
         return dict(I=I[o], J=J[o], cls=cls[o], phase=ph[o], exc=exc[o], hij=hij[o])
 
+    def connected_pairs_rows(self, rows):
+        """Pairs of the determinants `rows` (0-based psi_det indices) only, sorted by (I, J)."""
+        L = _lib.load()
+        r = np.ascontiguousarray(np.unique(np.asarray(rows)), dtype=np.int32)
+        n = C.c_int64()
+        check(L.qpgpu_connected_pairs_rows(self._ctx, _p(r), len(r), C.byref(n), None, None, None, None, None, None,
+                                           0), self._ctx)
+        P = n.value
+        I = np.empty(P, np.int32)
+        J = np.empty(P, np.int32)
+        cls = np.empty(P, np.int8)
+        ph = np.empty(P, np.int8)
+        exc = np.empty((P, 4), np.int16)
+        hij = np.empty(P)
+        check(L.qpgpu_connected_pairs_rows(self._ctx, _p(r), len(r), C.byref(n), _p(I), _p(J), _p(cls), _p(ph),
+                                           _p(exc), _p(hij), P), self._ctx)
+        o = np.lexsort((J, I))
+        return dict(I=I[o], J=J[o], cls=cls[o], phase=ph[o], exc=exc[o], hij=hij[o])
+
     # --- Davidson ------------------------------------------------------
     def davidson_diag_hs2(self, u_in, n_states, davidson_sze_max=8, threshold=1e-12, s2_eig=True,
                           precision=FP64, defect_every=0, preconditioner=0, max_iter=500, collect_every=0,
-                          collect_max=8, trace_cap=1024):
+                          collect_max=8, trace_cap=1024, algebra=0, state_following=False):
         """davidson_diag_hs2 (diagonalization_hs2.irp.f:1-49) on this determinant set.
 
         u_in: (N_st_diag, N) guess vectors (all of them, seeded by the caller).
@@ -180,7 +199,10 @@ class Wavefunction:
         preconditioner=1 uses the learned step (see mlp_*) in place of the
         diagonal one; preconditioner=2 adds it as an extra direction (in the
         correction slot of Ritz vector n_states + k); collect_every > 0
-        captures training pairs for it.  Returns dict(energies, s2, vectors,
+        captures training pairs for it.  algebra=ALGEBRA_FP64 keeps the
+        mixed modes' projections, Gram-Schmidt, Ritz vectors and step in FP64
+        (only sigma in FP32); state_following keeps the Ritz vectors that
+        overlap most with the guesses (the reference's EZFIO flag).  Returns dict(energies, s2, vectors,
         n_sigma, converged, n_fallback, n_samples, trace) with electronic energies.
         """
         u = np.ascontiguousarray(np.atleast_2d(u_in), dtype=np.float64).copy()
@@ -188,7 +210,8 @@ class Wavefunction:
         prm = _lib.DavidsonParams(n_states=n_states, n_states_diag=nsd, davidson_sze_max=davidson_sze_max,
                                   s2_eig=int(bool(s2_eig)), threshold=threshold, precision=precision,
                                   defect_every=defect_every, preconditioner=preconditioner, max_iter=max_iter,
-                                  collect_every=collect_every, collect_max=collect_max)
+                                  collect_every=collect_every, collect_max=collect_max,
+                                  state_following=int(bool(state_following)), algebra=algebra)
         prec = np.zeros(trace_cap, np.int32)
         en = np.zeros((trace_cap, n_states))
         rs = np.zeros((trace_cap, n_states))

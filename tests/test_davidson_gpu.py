@@ -87,3 +87,39 @@ def test_davidson_mixed_tight(prec_name, nsd, nst):
     np.testing.assert_allclose(rm["energies"][:nst], r64["energies"][:nst], rtol=0, atol=1e-9)
     tr = rm["trace"]
     assert (tr["precision"] == FP32).any() and tr["precision"][-1] == (FF if prec == FF else FP64)
+
+
+@pytest.mark.parametrize("threshold,tol", [(1e-10, 1e-6), (1e-12, 1e-9)])
+def test_davidson_mixed_fp64_algebra(threshold, tol):
+    # FP32 sigma with the FP64 sigma at each restart, every other operation
+    # (projections, Gram-Schmidt, Ritz vectors, step, residual norms) in FP64
+    from quantum_package_gb300 import ALGEBRA_FP64
+    from quantum_package_gb300.sigma import Wavefunction
+    p = G.make_problem(2, n_det=20_000, n_states=4)
+    wf = Wavefunction.from_problem(p)
+    u = _guess(p.n_det, 8, 3)
+    kw = dict(n_states=4, threshold=threshold, s2_eig=False, max_iter=500)
+    r64 = wf.davidson_diag_hs2(u, **kw)
+    rs = wf.davidson_diag_hs2(u, precision=FP32, algebra=ALGEBRA_FP64, **kw)
+    assert r64["converged"] and rs["converged"]
+    np.testing.assert_allclose(rs["energies"][:4], r64["energies"][:4], rtol=0, atol=tol)
+    tr = rs["trace"]
+    assert (tr["precision"] == FP32).any() and tr["precision"][-1] == FP64
+
+
+def test_davidson_state_following_matches_oracle():
+    # state_following (src/Davidson/EZFIO.cfg:19-22): the targets keep the
+    # Ritz vectors of largest overlap with the guesses
+    # (diagonalization_hs2.irp.f:328-370); same guess as the oracle's run
+    from quantum_package_gb300.sigma import Wavefunction
+    p = G.make_problem(1, n_det=3000)
+    wf = Wavefunction.from_problem(p)
+    o = Oracle.from_problem(p)
+    u = np.random.default_rng(1).normal(size=(4, p.n_det))
+    kw = dict(threshold=1e-10, s2_eig=False)
+    eo, _, _, _, _ = o.davidson(u, 2, davidson_sze_max=8, state_following=True, max_sigma=300, **kw)
+    eo_plain, _, _, _, _ = o.davidson(u, 2, davidson_sze_max=8, max_sigma=300, **kw)
+    assert abs(eo[0] - eo_plain[0]) > 1e-3  # the flag changes which states are followed here
+    r = wf.davidson_diag_hs2(u, n_states=2, davidson_sze_max=8, state_following=True, max_iter=300, **kw)
+    assert r["converged"]
+    np.testing.assert_allclose(r["energies"][:2], eo[:2], rtol=0, atol=1e-8)

@@ -205,3 +205,32 @@ def test_sigma_float_float_vs_fp64():
         a, b = v64.cpu().numpy(), vff.cpu().numpy()
         _assert_sigma(b.T, a.T, REL64, f"FF n_st={n_st}")
         _assert_sigma(sff.cpu().numpy().T, s64.cpu().numpy().T, REL64, f"FF S2 n_st={n_st}")
+
+
+def test_nonfinite_inputs_give_numeric_error():
+    # NaN / Inf in a host input vector: QPGPU_ERR_NUMERIC (-7) from every
+    # host-array entry point, and the context stays usable afterwards
+    p, o, wf = _problem(1, n_det=2_000)
+    u = G.random_coefficients(p.n_det, 2, p.seed)
+    bad = u.copy()
+    bad[1, 17] = np.nan
+    inf = u.copy()
+    inf[0, 3] = np.inf
+    for x in (bad, inf):
+        with pytest.raises(QPGPUError) as e:
+            wf.H_S2_u_0_nstates_openmp(x)
+        assert e.value.code == -7
+        with pytest.raises(QPGPUError) as e:
+            wf.u_0_H_u_0(x)
+        assert e.value.code == -7
+        order = wf.bilinear_order()
+        with pytest.raises(QPGPUError) as e:
+            wf.H_S2_u_0_nstates_openmp_work(np.ascontiguousarray(x[:, order].T), 1, p.n_det)
+        assert e.value.code == -7
+    g = np.random.default_rng(0).normal(size=(4, p.n_det))
+    g[2, 5] = np.nan
+    with pytest.raises(QPGPUError) as e:
+        wf.davidson_diag_hs2(g, n_states=1, s2_eig=False)
+    assert e.value.code == -7
+    v, _ = wf.H_S2_u_0_nstates_openmp(u)
+    _assert_sigma(v, o.h_s2_u0(u)[0], REL64, "after the refused calls")

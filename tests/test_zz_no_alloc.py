@@ -6,7 +6,9 @@ synchronisation of cudaMalloc/cudaFree.  This entry point keeps its scratch in
 a fixed array of the library instead.  The test calls it through the C-ABI,
 twice in a row, and checks it against qpgpu_sigma_bilinear (the regular entry
 point) at the tolerance of the other sigma tests; it also checks that a
-problem too large for the fixed scratch is refused with QPGPU_ERR_ARG.
+problem too large for the fixed scratch is refused with QPGPU_ERR_ARG, as are
+float-float requests, and that a direct-sigma set is refused with
+QPGPU_ERR_STATE.
 This file is collected last on purpose.
 """
 import ctypes as C
@@ -41,6 +43,9 @@ def test_noalloc_matches_regular_entry_point_twice(cfg, n_det, n_st):
     L = _lib.load()
     p = G.make_problem(cfg, n_det=n_det, n_states=n_st)
     wf = Wavefunction.from_problem(p)
+    if cfg == 2:
+        # rows split over several work chunks: the fixed scratch is really used
+        assert wf.info()["n_split_rows"] > 0
     u = torch.from_numpy(np.ascontiguousarray(G.random_coefficients(p.n_det, n_st, 7).T)).cuda()
     u32 = u.float()
     for prec in (FP64, FP32):
@@ -65,3 +70,32 @@ def test_noalloc_refuses_problems_beyond_its_scratch():
                                         C.c_void_p(u.data_ptr()), None, 8, FP64, None)
     assert rc == -1
     assert b"scratch" in L.qpgpu_last_error(wf.ctx)
+
+
+def test_noalloc_first_fp32_call_and_refusals():
+    # an FP32 call on a fresh context (no FP32 launch shape tuned yet) runs the
+    # default shape; float-float precision and direct-sigma sets are refused
+    import torch
+    from quantum_package_gb300 import FF, SIGMA_DIRECT
+    from quantum_package_gb300.sigma import Wavefunction
+    L = _lib.load()
+    p = G.make_problem(2, n_det=20_000, n_states=2)
+    wf = Wavefunction.from_problem(p)
+    u = torch.from_numpy(np.ascontiguousarray(G.random_coefficients(p.n_det, 2, 9).T)).cuda()
+    u32 = u.float()
+    v, s = _sigma(L, wf, L.qpgpu_sigma_bilinear_noalloc, u, u32, FP32)
+    ref_v, ref_s = _sigma(L, wf, L.qpgpu_sigma_bilinear, u, u32, FP32)
+    assert np.abs(v - ref_v).max() <= REL[FP32] * np.abs(ref_v).max()
+    assert np.abs(s - ref_s).max() <= REL[FP32] * max(1.0, np.abs(ref_s).max())
+    out = torch.empty_like(u)
+    rc = L.qpgpu_sigma_bilinear_noalloc(wf.ctx, C.c_void_p(out.data_ptr()), C.c_void_p(out.data_ptr()),
+                                        C.c_void_p(u.data_ptr()), C.c_void_p(u32.data_ptr()), 2, FF, None)
+    assert rc == -1  # QPGPU_ERR_ARG
+    q = G.make_problem(1, n_det=3_000)
+    wd = Wavefunction.from_problem(q, sigma_mode=SIGMA_DIRECT)
+    ud = torch.zeros((q.n_det, 1), dtype=torch.float64, device="cuda")
+    vd = torch.empty_like(ud)
+    rc = L.qpgpu_sigma_bilinear_noalloc(wd.ctx, C.c_void_p(vd.data_ptr()), C.c_void_p(vd.data_ptr()),
+                                        C.c_void_p(ud.data_ptr()), None, 1, FP64, None)
+    assert rc == -2  # QPGPU_ERR_STATE
+    assert b"stored pairs" in L.qpgpu_last_error(wd.ctx)
