@@ -161,6 +161,23 @@ int qpgpu_sigma_bilinear(qpgpu_ctx* ctx, double* v_t, double* s_t, const double*
 int qpgpu_sigma_bilinear_noalloc(qpgpu_ctx* ctx, double* v_t, double* s_t, const double* u_t,
                                  const float* u_t32, int n_st, int precision, void* stream);
 
+/* Dressing of one state for the MRCC / MRCEPA0 sigma, H_S2_u_0_mrcc_nstates
+ * (plugins/MRCC_Utils/davidson.irp.f:955-1127), host arrays: determinants
+ * idx_ref[0..n_ref) (psi_det indices, 0-based; idx_ref of the reference) and
+ * idx_non_ref[0..n_non_ref) (idx_non_ref), all distinct; delta_ij and
+ * delta_ij_s2 (n_non_ref, n_ref) column-major, the slice delta_ij(istate,:,:)
+ * of the reference's provider; delta_ii (n_ref, may be NULL for zeros), the
+ * diagonal dressing davidson_diag_mrcc_hs2 adds to H_jj (:547-549).  The
+ * dressing stays with the determinant set (qpgpu_set_dets drops it). */
+int qpgpu_set_dressing(qpgpu_ctx* ctx, int n_ref, const int32_t* idx_ref, int64_t n_non_ref,
+                       const int32_t* idx_non_ref, const double* delta_ij, const double* delta_ij_s2,
+                       const double* delta_ii);
+int qpgpu_clear_dressing(qpgpu_ctx* ctx);
+
+/* H_S2_u_0_mrcc_nstates with host arrays, as qpgpu_h_s2_u0: v_0 = (H + dressing) u_0,
+ * s_0 = (S^2 + dressing_s2) u_0, the diagonal of H dressed by delta_ii. */
+int qpgpu_h_s2_u0_dressed(qpgpu_ctx* ctx, double* v0, double* s0, const double* u0, int n_st, int64_t ld);
+
 /* Davidson parameters: the EZFIO knobs of src/Davidson/EZFIO.cfg:1-36 and
  * src/Determinants/EZFIO.cfg:13-41 plus the precision options. */
 typedef struct qpgpu_davidson_params {
@@ -183,6 +200,9 @@ typedef struct qpgpu_davidson_params {
                                Ritz vectors and the step on the FP32 pipes (float-float / FP32);
                                QPGPU_ALGEBRA_FP64 keeps them in FP64 as in the plain loop, so only
                                sigma runs in FP32 */
+  int32_t dressed;          /* 1: davidson_diag_mrcc_hs2 (plugins/MRCC_Utils/davidson.irp.f:496-553):
+                               sigma and H_jj carry the context's dressing (qpgpu_set_dressing) */
+  int32_t reserved;         /* 0 */
 } qpgpu_davidson_params;
 #define QPGPU_ALGEBRA_FAST 0
 #define QPGPU_ALGEBRA_FP64 1

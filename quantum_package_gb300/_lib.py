@@ -41,7 +41,7 @@ class DavidsonParams(C.Structure):
                 ("s2_eig", C.c_int32), ("threshold", C.c_double), ("precision", C.c_int32),
                 ("defect_every", C.c_int32), ("preconditioner", C.c_int32), ("max_iter", C.c_int32),
                 ("collect_every", C.c_int32), ("collect_max", C.c_int32), ("state_following", C.c_int32),
-                ("algebra", C.c_int32)]
+                ("algebra", C.c_int32), ("dressed", C.c_int32), ("reserved", C.c_int32)]
 
 
 class DavidsonTrace(C.Structure):
@@ -93,6 +93,9 @@ def load():
         "qpgpu_sigma_bilinear": (C.c_int, [vp, vp, vp, vp, vp, C.c_int, C.c_int, vp]),
         "qpgpu_sigma_bilinear_noalloc": (C.c_int, [vp, vp, vp, vp, vp, C.c_int, C.c_int, vp]),
         "qpgpu_bilinear_order": (C.c_int, [vp, vp]),
+        "qpgpu_set_dressing": (C.c_int, [vp, C.c_int, vp, C.c_int64, vp, vp, vp, vp]),
+        "qpgpu_clear_dressing": (C.c_int, [vp]),
+        "qpgpu_h_s2_u0_dressed": (C.c_int, [vp, vp, vp, vp, C.c_int, C.c_int64]),
         "qpgpu_batch_create": (C.c_int, [vp, C.c_int, C.POINTER(vp)]),
         "qpgpu_batch_destroy": (C.c_int, [vp]),
         "qpgpu_batch_last_error": (C.c_char_p, [vp]),

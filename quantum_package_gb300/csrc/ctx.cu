@@ -250,6 +250,7 @@ int qpgpu_destroy(qpgpu_ctx* c) {
     Lock l(c->mu);
     cudaStreamSynchronize(c->stream);
     c->items.free_all();
+    qp_free_dressing(c);
     qp_free_pairs(c);
     qp_free_dets(c);
     free_ints(c);
@@ -309,6 +310,7 @@ int qpgpu_set_integrals(qpgpu_ctx* c, const double* h, const double* eri) {
       if (h[i + (size_t)j * n] != h[j + (size_t)i * n])
         return qpgpu_fail(c, QPGPU_ERR_ARG, "h_pq must be symmetric");
   c->items.free_all();
+  qp_free_dressing(c);
   qp_free_pairs(c);
   qp_free_dets(c);
   free_ints(c);
@@ -380,6 +382,7 @@ int qpgpu_set_dets(qpgpu_ctx* c, const uint64_t* psi_det, int64_t n_det) {
     }
   }
   c->items.free_all();
+  qp_free_dressing(c);
   qp_free_pairs(c);
   qp_free_dets(c);
   cudaStream_t st = c->stream;
@@ -438,7 +441,7 @@ namespace {
 // qpgpu_h_s2_u0_device with an optional device flag that the input conversion
 // sets when u0 holds a NaN or an infinity (called with the context locked)
 int h_s2_u0_dev(qpgpu_ctx* c, double* v0, double* s0, const double* u0, int n_st, int64_t ld, int precision,
-                cudaStream_t st, int* bad) {
+                cudaStream_t st, int* bad, bool dressed = false) {
   const int64_t N = c->N;
   int rc = 0;
   const int nb = n_st < 8 ? n_st : 8;
@@ -453,6 +456,7 @@ int h_s2_u0_dev(qpgpu_ctx* c, double* v0, double* s0, const double* u0, int n_st
     qp_to_bilinear(u0 + (int64_t)s0i * ld, ld, c->d_order, ut, precision == QPGPU_FP32 ? ut32 : nullptr, m, N, st,
                    bad);
     rc = qp_sigma_launch(c, &c->items, vt, stt, ut, ut32, m, precision, st, 0, (int)N, 0, 1);
+    if (!rc && dressed) rc = qp_dress(c, vt, stt, ut, m, st);
     if (rc) return rc;
     qp_from_bilinear(vt, ld, c->d_order, v0 + (int64_t)s0i * ld, m, N, st);
     qp_from_bilinear(stt, ld, c->d_order, s0 + (int64_t)s0i * ld, m, N, st);
@@ -474,7 +478,8 @@ int qpgpu_h_s2_u0_device(qpgpu_ctx* c, double* v0, double* s0, const double* u0,
   return h_s2_u0_dev(c, v0, s0, u0, n_st, ld, precision, stream ? (cudaStream_t)stream : c->stream, nullptr);
 }
 
-int qpgpu_h_s2_u0(qpgpu_ctx* c, double* v0, double* s0, const double* u0, int n_st, int64_t ld) {
+namespace {
+int h_s2_u0_host(qpgpu_ctx* c, double* v0, double* s0, const double* u0, int n_st, int64_t ld, bool dressed) {
   int rc = check_ctx(c, true, true);
   if (rc) return rc;
   if (!v0 || !s0 || !u0 || n_st < 1 || ld < c->N) return qpgpu_fail(c, QPGPU_ERR_ARG, "bad h_s2_u0 arguments");
@@ -497,7 +502,8 @@ int qpgpu_h_s2_u0(qpgpu_ctx* c, double* v0, double* s0, const double* u0, int n_
   if (cudaMemcpy2DAsync(du, N * sizeof(double), u0, ld * sizeof(double), N * sizeof(double), n_st,
                         cudaMemcpyHostToDevice, st) != cudaSuccess)
     rc = qpgpu_fail(c, QPGPU_ERR_CUDA, "copy of u_0 failed");
-  if (!rc) rc = h_s2_u0_dev(c, dv, ds, du, n_st, N, QPGPU_FP64, st, bad);
+  if (!rc && dressed && !c->dress.on) rc = qpgpu_fail(c, QPGPU_ERR_STATE, "no dressing set");
+  if (!rc) rc = h_s2_u0_dev(c, dv, ds, du, n_st, N, QPGPU_FP64, st, bad, dressed);
   if (!rc && (cudaMemcpy2DAsync(v0, ld * sizeof(double), dv, N * sizeof(double), N * sizeof(double), n_st,
                                 cudaMemcpyDeviceToHost, st) != cudaSuccess ||
               cudaMemcpy2DAsync(s0, ld * sizeof(double), ds, N * sizeof(double), N * sizeof(double), n_st,
@@ -508,6 +514,16 @@ int qpgpu_h_s2_u0(qpgpu_ctx* c, double* v0, double* s0, const double* u0, int n_
   if (!rc && e != cudaSuccess) rc = qpgpu_fail(c, QPGPU_ERR_CUDA, cudaGetErrorString(e));
   if (!rc && hbad) rc = qpgpu_fail(c, QPGPU_ERR_NUMERIC, "u_0 holds a NaN or an infinity");
   return rc;
+}
+
+}  // namespace
+
+int qpgpu_h_s2_u0(qpgpu_ctx* c, double* v0, double* s0, const double* u0, int n_st, int64_t ld) {
+  return h_s2_u0_host(c, v0, s0, u0, n_st, ld, false);
+}
+
+int qpgpu_h_s2_u0_dressed(qpgpu_ctx* c, double* v0, double* s0, const double* u0, int n_st, int64_t ld) {
+  return h_s2_u0_host(c, v0, s0, u0, n_st, ld, true);
 }
 
 namespace {

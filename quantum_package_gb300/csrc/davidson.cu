@@ -1308,6 +1308,7 @@ extern "C" int qpgpu_davidson_hs2(qpgpu_ctx* c, double* u_in, int64_t dim_in, do
     return qpgpu_fail(c, QPGPU_ERR_ARG, "bad Davidson parameters (1 <= n_states <= n_states_diag <= 8)");
   if (prm->algebra != QPGPU_ALGEBRA_FAST && prm->algebra != QPGPU_ALGEBRA_FP64)
     return qpgpu_fail(c, QPGPU_ERR_ARG, "algebra must be QPGPU_ALGEBRA_FAST or QPGPU_ALGEBRA_FP64");
+  if (prm->dressed && !c->dress.on) return qpgpu_fail(c, QPGPU_ERR_STATE, "dressed Davidson without a dressing");
   if (prm->preconditioner < 0 || prm->preconditioner > 2)
     return qpgpu_fail(c, QPGPU_ERR_ARG, "preconditioner must be 0 (diagonal), 1 (learned) or 2 (learned, extra direction)");
   if ((int64_t)nsd * 3 > N) return qpgpu_fail(c, QPGPU_ERR_ARG, "N_st_diag*3 > sze (diagonalization_hs2.irp.f:110)");
@@ -1399,6 +1400,7 @@ extern "C" int qpgpu_davidson_hs2(qpgpu_ctx* c, double* u_in, int64_t dim_in, do
       return qpgpu_fail(c, QPGPU_ERR_NUMERIC, "the guess vectors hold a NaN or an infinity");
     }
   }
+  const double* hjj = prm->dressed ? c->dress.hdress : c->d_hdiag;  // dressed H_jj (:547-549)
   const double Sz = 0.5 * (c->na - c->nb);
   const double sz2sz = Sz * (Sz - 1.0), expected_s2 = Sz * (Sz + 1.0);
   const int mmax = itermax * nsd;
@@ -1438,6 +1440,7 @@ extern "C" int qpgpu_davidson_hs2(qpgpu_ctx* c, double* u_in, int64_t dim_in, do
                    ? qp_sigma_ff(c, &c->items, d.blk(d.W, b), d.blk(d.S, b), d.blk(d.U, b), nsd, st, 0, (int)N, 0, 1)
                    : qp_sigma_launch(c, &c->items, d.blk(d.W, b), d.blk(d.S, b), d.blk(d.U, b), d.u32, nsd, prec, st,
                                      0, (int)N, 0, 1, qp_pad_states(nsd));
+      if (!rc && prm->dressed) rc = qp_dress(c, d.blk(d.W, b), d.blk(d.S, b), d.blk(d.U, b), nsd, st);
       if (rc) return rc;
       ++n_sigma;
       prof.mark(DavProf::SIGMA);
@@ -1553,7 +1556,7 @@ extern "C" int qpgpu_davidson_hs2(qpgpu_ctx* c, double* u_in, int64_t dim_in, do
       sp.nst = nst;
       ++it_global;
       if (collect_every && n_cap < collect_max && it_global >= 2 && (it_global - 2) % collect_every == 0) {
-        k_capture<<<gsz(N), DBLK, 0, st>>>(d.blk(d.U, iter), d.blk(d.W, iter), d.blk(d.S, iter), c->d_hdiag,
+        k_capture<<<gsz(N), DBLK, 0, st>>>(d.blk(d.U, iter), d.blk(d.W, iter), d.blk(d.S, iter), hjj,
                                            (const float4*)c->d_detfeat, N, sp, n_cap * nst, d.cX, d.cd, d.cc);
         ++n_cap;
       }
@@ -1561,17 +1564,17 @@ extern "C" int qpgpu_davidson_hs2(qpgpu_ctx* c, double* u_in, int64_t dim_in, do
       for (int k = 0; k < nst; ++k)
         if (mlp_on[k]) mask |= 1u << k;
       if (mask) {
-        k_mlp_features<<<gsz(N), DBLK, 0, st>>>(d.blk(d.U, iter), d.blk(d.W, iter), d.blk(d.S, iter), c->d_hdiag,
+        k_mlp_features<<<gsz(N), DBLK, 0, st>>>(d.blk(d.U, iter), d.blk(d.W, iter), d.blk(d.S, iter), hjj,
                                                 (const float4*)c->d_detfeat, N, sp, d.mlpX);
         qp_mlp_eval(c->mlp.params, d.mlpX, d.mlpG, N * nst, st, c->n_sm);
-        k_step_mlp<<<d.ncta, DBLK, 0, st>>>(d.blk(d.U, iter), d.blk(d.W, iter), d.blk(d.S, iter), c->d_hdiag, d.mlpG,
+        k_step_mlp<<<d.ncta, DBLK, 0, st>>>(d.blk(d.U, iter), d.blk(d.W, iter), d.blk(d.S, iter), hjj, d.mlpG,
                                             N, sp, mask, mlp_extra, d.part);
       }
       else if (ffalg)
-        k_step_mixed<<<d.ncta, DBLK, 0, st>>>(d.blk(d.U, iter), d.blk(d.W, iter), d.blk(d.S, iter), c->d_hdiag, N, sp,
+        k_step_mixed<<<d.ncta, DBLK, 0, st>>>(d.blk(d.U, iter), d.blk(d.W, iter), d.blk(d.S, iter), hjj, N, sp,
                                               d.part);
       else
-        k_step<<<d.ncta, DBLK, 0, st>>>(d.blk(d.U, iter), d.blk(d.W, iter), d.blk(d.S, iter), c->d_hdiag, N, sp, d.part);
+        k_step<<<d.ncta, DBLK, 0, st>>>(d.blk(d.U, iter), d.blk(d.W, iter), d.blk(d.S, iter), hjj, N, sp, d.part);
       QP_CUDA(c, cudaGetLastError());
       QP_CUDA(c, cudaMemcpyAsync(partial.data(), d.part, partial.size() * sizeof(double), cudaMemcpyDeviceToHost, st));
       QP_CUDA(c, cudaStreamSynchronize(st));

@@ -354,6 +354,19 @@ struct MlpState {
   }
 };
 
+// Dressing of one state (qpgpu_set_dressing), determinants as bilinear positions
+struct Dressing {
+  bool on = false;
+  int n_ref = 0;
+  int64_t n_nref = 0;
+  int* ref = nullptr;        // (n_ref)
+  int* nref = nullptr;       // (n_nref)
+  double* d = nullptr;       // delta_ij (n_nref, n_ref) column-major
+  double* ds = nullptr;      // delta_ij_s2
+  double* dii = nullptr;     // delta_ii (n_ref)
+  double* hdress = nullptr;  // H_jj with delta_ii added at the references (N)
+};
+
 struct qpgpu_ctx {
   std::mutex mu;
   int device = 0;
@@ -423,6 +436,7 @@ struct qpgpu_ctx {
   double setup_ms = 0.0;
   SigmaItems items;
   MlpState mlp;
+  Dressing dress;
   float* d_detfeat = nullptr;  // (N, 4): alpha rank, beta rank, orbital-energy sum, log10(sum_J H_IJ^2)/4
   // optional phase timing of the set-up (environment QPGPU_PROFILE=1)
   bool profile = false;
@@ -492,6 +506,11 @@ inline void qp_mark(qpgpu_ctx* c, const char* name) {
   c->marks.emplace_back(name, e);
 }
 void qp_report_marks(qpgpu_ctx* c);  // ctx.cu
+
+// dressing (dress.cu): adds the context's dressing to a bilinear-layout sigma
+// v, s of u (nst states fastest); no-op without a dressing
+int qp_dress(qpgpu_ctx* c, double* v, double* s, const double* u, int nst, cudaStream_t st);
+void qp_free_dressing(qpgpu_ctx* c);
 
 // learned preconditioner (mlp.cu)
 int qp_det_features(qpgpu_ctx* c);

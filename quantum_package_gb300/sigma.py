@@ -165,6 +165,32 @@ class Wavefunction:
         o = np.lexsort((J, I))
         return dict(I=I[o], J=J[o], cls=cls[o], phase=ph[o], exc=exc[o], hij=hij[o])
 
+    # --- dressing (MRCC / MRCEPA0) ---------------------------------------
+    def set_dressing(self, idx_ref, idx_non_ref, delta_ij, delta_ij_s2, delta_ii=None):
+        """Dressing of one state (delta_ij(istate,:,:) of the reference's providers):
+        idx_ref (n_ref,), idx_non_ref (n_non_ref,) psi_det indices (0-based);
+        delta_ij, delta_ij_s2 arrays (n_ref, n_non_ref) [the Fortran (n_non_ref, n_ref)];
+        delta_ii (n_ref,) or None."""
+        r = np.ascontiguousarray(idx_ref, np.int32)
+        nr = np.ascontiguousarray(idx_non_ref, np.int32)
+        d = np.ascontiguousarray(delta_ij, np.float64)
+        ds = np.ascontiguousarray(delta_ij_s2, np.float64)
+        assert d.shape == (len(r), len(nr)) and ds.shape == d.shape
+        dii = None if delta_ii is None else np.ascontiguousarray(delta_ii, np.float64)
+        check(_lib.load().qpgpu_set_dressing(self._ctx, len(r), _p(r), len(nr), _p(nr), _p(d), _p(ds), _p(dii)),
+              self._ctx)
+
+    def clear_dressing(self):
+        check(_lib.load().qpgpu_clear_dressing(self._ctx), self._ctx)
+
+    def H_S2_u_0_mrcc_nstates(self, u_0):
+        """H_S2_u_0_mrcc_nstates (plugins/MRCC_Utils/davidson.irp.f:955): sigma of H plus the dressing."""
+        u = np.ascontiguousarray(np.atleast_2d(u_0), dtype=np.float64)
+        v = np.empty_like(u)
+        s = np.empty_like(u)
+        check(_lib.load().qpgpu_h_s2_u0_dressed(self._ctx, _p(v), _p(s), _p(u), u.shape[0], u.shape[1]), self._ctx)
+        return v, s
+
     def connected_pairs_rows(self, rows):
         """Pairs of the determinants `rows` (0-based psi_det indices) only, sorted by (I, J)."""
         L = _lib.load()
@@ -187,7 +213,7 @@ class Wavefunction:
     # --- Davidson ------------------------------------------------------
     def davidson_diag_hs2(self, u_in, n_states, davidson_sze_max=8, threshold=1e-12, s2_eig=True,
                           precision=FP64, defect_every=0, preconditioner=0, max_iter=500, collect_every=0,
-                          collect_max=8, trace_cap=1024, algebra=0, state_following=False):
+                          collect_max=8, trace_cap=1024, algebra=0, state_following=False, dressed=False):
         """davidson_diag_hs2 (diagonalization_hs2.irp.f:1-49) on this determinant set.
 
         u_in: (N_st_diag, N) guess vectors (all of them, seeded by the caller).
@@ -202,7 +228,8 @@ class Wavefunction:
         captures training pairs for it.  algebra=ALGEBRA_FP64 keeps the
         mixed modes' projections, Gram-Schmidt, Ritz vectors and step in FP64
         (only sigma in FP32); state_following keeps the Ritz vectors that
-        overlap most with the guesses (the reference's EZFIO flag).  Returns dict(energies, s2, vectors,
+        overlap most with the guesses (the reference's EZFIO flag); dressed
+        runs davidson_diag_mrcc_hs2 with the context's dressing.  Returns dict(energies, s2, vectors,
         n_sigma, converged, n_fallback, n_samples, trace) with electronic energies.
         """
         u = np.ascontiguousarray(np.atleast_2d(u_in), dtype=np.float64).copy()
@@ -211,7 +238,8 @@ class Wavefunction:
                                   s2_eig=int(bool(s2_eig)), threshold=threshold, precision=precision,
                                   defect_every=defect_every, preconditioner=preconditioner, max_iter=max_iter,
                                   collect_every=collect_every, collect_max=collect_max,
-                                  state_following=int(bool(state_following)), algebra=algebra)
+                                  state_following=int(bool(state_following)), algebra=algebra,
+                                  dressed=int(bool(dressed)))
         prec = np.zeros(trace_cap, np.int32)
         en = np.zeros((trace_cap, n_states))
         rs = np.zeros((trace_cap, n_states))
