@@ -278,7 +278,7 @@ def davidson_block(prob, wf):
     block's settings, the raw runs and the tight FP64 run whose eigenvectors the
     oracle checks; davidson_finish turns the runs into times against the
     oracle's energies."""
-    from quantum_package_gb300 import ALGEBRA_FP64, FF, FP32
+    from quantum_package_gb300 import ALGEBRA_FP64, ALGEBRA_TC, FF, FP32
     N = prob.n_det
     u = _guess(N, prob.seed)
     kw = dict(n_states=N_STATES, s2_eig=False, max_iter=400, davidson_sze_max=SZE_MAX)
@@ -299,6 +299,8 @@ def davidson_block(prob, wf):
     # the specification's split: FP32 sigma with the FP64 sigma at each restart,
     # projections, Gram-Schmidt, Ritz vectors, step and residual norms in FP64
     run("mixed_spec", precision=FP32, algebra=ALGEBRA_FP64)
+    # the same split with the FP64-accurate Gram blocks on the tensor cores
+    run("mixed_spec_tc", precision=FP32, algebra=ALGEBRA_TC)
     # restart (defect-correction) sigma in float-float instead of FP64
     run("mixed_ff_restart", precision=FF)
     # learned preconditioner: earlier stages of the same determinant draw

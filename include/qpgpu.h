@@ -35,8 +35,7 @@ extern "C" {
 #define QPGPU_ERR_CUDA (-3)     /* CUDA runtime error */
 #define QPGPU_ERR_NOMEM (-4)    /* device allocation failed */
 #define QPGPU_ERR_DAVIDSON (-5) /* Davidson failed (residual > 1e8) */
-#define QPGPU_ERR_TIMEOUT (-6)  /* reserved for bounded device waits (no entry point waits on a device
-                                   flag in this version, so none returns it) */
+#define QPGPU_ERR_TIMEOUT (-6)  /* a bounded device wait ran out (the tensor-core Gram's mbarrier waits) */
 #define QPGPU_ERR_NUMERIC (-7)  /* NaN / Inf in an input vector: checked by the entry points that take
                                    host arrays (qpgpu_h_s2_u0, _work, qpgpu_u0_h_u0 and the guess of
                                    qpgpu_davidson_hs2); the asynchronous device entry points do not check */
@@ -178,6 +177,21 @@ int qpgpu_clear_dressing(qpgpu_ctx* ctx);
  * s_0 = (S^2 + dressing_s2) u_0, the diagonal of H dressed by delta_ii. */
 int qpgpu_h_s2_u0_dressed(qpgpu_ctx* ctx, double* v0, double* s0, const double* u0, int n_st, int64_t ld);
 
+/* X(m, n) = A^T B for tall A (N x m) and B (N x n), device arrays whose rows
+ * are lda / ldb doubles apart (the u_t(N_st, N) layout, states fastest), on
+ * the given stream (NULL: the context's): the dgemm('T','N') Gram blocks of
+ * davidson_diag_hjj_sjj (src/Davidson/diagonalization_hs2.irp.f:232-238)
+ * computed to FP64 accuracy on the tensor cores.  Each column is split into
+ * eight balanced 7-bit BF16 digit planes against its largest exponent (Ozaki
+ * splitting), the digit products are summed exactly (FP32 tensor-core
+ * accumulators flushed into integers every 128 rows) and the per-SM results
+ * combined in FP64.  m <= 128, n <= 16; X (m x n, row-major) is written on
+ * the device and the call waits for the stream; a bounded tensor-core wait
+ * that runs out gives QPGPU_ERR_TIMEOUT.  Uses the context only for its
+ * scratch and stream. */
+int qpgpu_gram_tc(qpgpu_ctx* ctx, const double* A, int64_t lda, int m, const double* B, int64_t ldb, int n,
+                  int64_t N, double* X, void* stream);
+
 /* Davidson parameters: the EZFIO knobs of src/Davidson/EZFIO.cfg:1-36 and
  * src/Determinants/EZFIO.cfg:13-41 plus the precision options. */
 typedef struct qpgpu_davidson_params {
@@ -196,16 +210,21 @@ typedef struct qpgpu_davidson_params {
   int32_t collect_max;      /* captures kept (default 8) */
   int32_t state_following;  /* state_following (src/Davidson/EZFIO.cfg:19-22): keep the Ritz vectors
                                that overlap most with the guess states (diagonalization_hs2.irp.f:328-370) */
-  int32_t algebra;          /* mixed modes only: QPGPU_ALGEBRA_FAST runs the projections, Gram-Schmidt,
-                               Ritz vectors and the step on the FP32 pipes (float-float / FP32);
-                               QPGPU_ALGEBRA_FP64 keeps them in FP64 as in the plain loop, so only
-                               sigma runs in FP32 */
+  int32_t algebra;          /* QPGPU_ALGEBRA_FAST (mixed modes): projections, Gram-Schmidt, Ritz vectors
+                               and the step on the FP32 pipes (float-float / FP32); QPGPU_ALGEBRA_FP64:
+                               all of them in FP64 as in the plain loop, so only sigma runs in FP32;
+                               QPGPU_ALGEBRA_TC (any precision): FP64-accurate with the Gram blocks
+                               (projections, Gram-Schmidt and Cholesky-QR Grams) on the tensor cores
+                               (qpgpu_gram_tc's splitting), updates, step and residual norms in FP64,
+                               the Ritz vectors of FP32-sigma iterations in FP32 (they only feed the
+                               step) */
   int32_t dressed;          /* 1: davidson_diag_mrcc_hs2 (plugins/MRCC_Utils/davidson.irp.f:496-553):
                                sigma and H_jj carry the context's dressing (qpgpu_set_dressing) */
   int32_t reserved;         /* 0 */
 } qpgpu_davidson_params;
 #define QPGPU_ALGEBRA_FAST 0
 #define QPGPU_ALGEBRA_FP64 1
+#define QPGPU_ALGEBRA_TC 2
 
 /* Optional per-iteration record of a Davidson run. */
 typedef struct qpgpu_davidson_trace {

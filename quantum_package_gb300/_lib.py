@@ -18,7 +18,7 @@ ERRORS = {
 }
 FP64, FP32, FF = 0, 1, 2
 SIGMA_AUTO, SIGMA_STORED, SIGMA_DIRECT = 0, 1, 2  # qpgpu_set_sigma_mode
-ALGEBRA_FAST, ALGEBRA_FP64 = 0, 1  # qpgpu_davidson_params.algebra
+ALGEBRA_FAST, ALGEBRA_FP64, ALGEBRA_TC = 0, 1, 2  # qpgpu_davidson_params.algebra
 
 HEADER = os.path.join(os.path.dirname(os.path.dirname(os.path.abspath(__file__))), "include", "qpgpu.h")
 
@@ -96,6 +96,7 @@ def load():
         "qpgpu_set_dressing": (C.c_int, [vp, C.c_int, vp, C.c_int64, vp, vp, vp, vp]),
         "qpgpu_clear_dressing": (C.c_int, [vp]),
         "qpgpu_h_s2_u0_dressed": (C.c_int, [vp, vp, vp, vp, C.c_int, C.c_int64]),
+        "qpgpu_gram_tc": (C.c_int, [vp, vp, C.c_int64, C.c_int, vp, C.c_int64, C.c_int, C.c_int64, vp, vp]),
         "qpgpu_batch_create": (C.c_int, [vp, C.c_int, C.POINTER(vp)]),
         "qpgpu_batch_destroy": (C.c_int, [vp]),
         "qpgpu_batch_last_error": (C.c_char_p, [vp]),

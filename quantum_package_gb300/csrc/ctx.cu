@@ -260,6 +260,7 @@ int qpgpu_destroy(qpgpu_ctx* c) {
     dev_free(c->d_ffu);
     dev_free(c->d_direct_ut);
     dev_free(c->d_flag);
+    dev_free(c->d_tc_scratch);
     cudaStreamDestroy(c->stream);
   }
   delete c;

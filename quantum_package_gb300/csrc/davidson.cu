@@ -995,6 +995,12 @@ struct Dav {
   int64_t sUf = 0;                       // block stride of Uf (float2)
   int ncta = 0;
   int64_t rows_per_cta = 0;
+  // tensor-core Gram blocks (QPGPU_ALGEBRA_TC): biased max exponents of the
+  // columns of the finished U blocks, of the current B operand, and the
+  // status flag of the bounded tensor-core waits
+  bool tc = false;
+  int* uexp = nullptr;  // [MAXM]
+  int* bexp = nullptr;  // [2 MAXS + 1]: B exponents, then the status flag
   ~Dav() {
     dev_free(U);
     dev_free(W);
@@ -1010,6 +1016,8 @@ struct Dav {
     dev_free(mlpG);
     dev_free(Uf);
     dev_free(Bf);
+    dev_free(uexp);
+    dev_free(bexp);
   }
   double* blk(double* X, int b) const { return X + (int64_t)b * N * nsd; }
 };
@@ -1053,6 +1061,27 @@ int gram(Dav& d, const double* A, int m, const double* B0, const double* B1, dou
 #undef QP_GRAM_CASE
   k_reduce_partials<<<gsz((int64_t)m * nbc * 32), DBLK, 0, d.st>>>(d.part, d.ncta, m * nbc, out, skip);
   return 0;
+}
+
+// out (m x nbc) = A^T [B0 (B1)] on the tensor cores (FP64-accurate Ozaki
+// splitting, ozaki.cu).  The exponents of B0 / B1 are computed here; those
+// of A are, by `amode`: TC_BASIS, the cached ones of finished U blocks
+// (d.uexp); TC_BASIS_NEW, the same with B0 as A's last block (Gram-Schmidt
+// of the new block against the basis that holds it); TC_SELF, A = B0.
+enum { TC_BASIS, TC_BASIS_NEW, TC_SELF };
+void gram_tc(Dav& d, const double* A, int m, const double* B0, const double* B1, double* out, int amode,
+             const int* skip = nullptr) {
+  const int nbc = d.nsd * (B1 ? 2 : 1);
+  int* eB = d.bexp;
+  cudaMemsetAsync(eB, 0, nbc * sizeof(int), d.st);
+  qp_col_maxexp(B0, 1, 0, d.nsd, d.nsd, d.N, eB, 0, skip, d.st, d.c->n_sm);
+  if (B1) qp_col_maxexp(B1, 1, 0, d.nsd, d.nsd, d.N, eB, d.nsd, skip, d.st, d.c->n_sm);
+  const int* eA = amode == TC_SELF ? eB : d.uexp;
+  if (amode == TC_BASIS_NEW)
+    cudaMemcpyAsync(d.uexp + (m - d.nsd), eB, d.nsd * sizeof(int), cudaMemcpyDeviceToDevice, d.st);
+  qp_gram_oz(A, d.N * d.nsd, m, d.nsd, d.nsd, B0, B1, nbc, d.nsd, d.nsd, d.N, eA, eB, d.part, d.c->n_sm, skip,
+             d.bexp + 2 * MAXS, d.st);
+  qp_oz_reduce(d.part, d.c->n_sm, m * nbc, out, skip, d.st);
 }
 
 // float-float copy of one block (X1 = nullptr) or of [X0 X1]
@@ -1220,6 +1249,25 @@ void orthonormalise(Dav& d, int b, bool ff) {
   double* Rinv = d.small + OFF_RINV;
   int* skip2 = (int*)(d.small + OFF_FLAG);
   const int m = b * d.nsd, m1 = m + d.nsd;
+  if (d.tc) {  // Gram blocks on the tensor cores, updates in FP64
+    if (b > 0) {
+      gram_tc(d, d.U, m1, Ub, nullptr, X, TC_BASIS_NEW);
+      k_cgs_coef<<<1, 128, 0, d.st>>>(X, m, d.nsd, K, skip2, 0);
+      lincomb(d, m1, K, d.U, Ub);
+      gram_tc(d, d.U, m1, Ub, nullptr, X, TC_BASIS_NEW, skip2);
+      k_cgs_coef<<<1, 128, 0, d.st>>>(X, m, d.nsd, K, skip2, 1);
+      lincomb(d, m1, K, d.U, Ub, nullptr, nullptr, nullptr, nullptr, skip2);
+    }
+    for (int pass = (b > 0) ? 1 : 0; pass < 2; ++pass) {
+      gram_tc(d, Ub, d.nsd, Ub, nullptr, G, TC_SELF);
+      k_chol_inv<<<1, 32, 0, d.st>>>(G, d.nsd, Rinv);
+      lincomb(d, d.nsd, Rinv, Ub, Ub);
+    }
+    // the block is final: cache its column exponents for later Grams
+    cudaMemsetAsync(d.uexp + m, 0, d.nsd * sizeof(int), d.st);
+    qp_col_maxexp(Ub, 1, 0, d.nsd, d.nsd, d.N, d.uexp, m, nullptr, d.st, d.c->n_sm);
+    return;
+  }
   if (!ff) {
     if (b > 0) {
       gram(d, d.U, m1, Ub, nullptr, X);
@@ -1306,8 +1354,8 @@ extern "C" int qpgpu_davidson_hs2(qpgpu_ctx* c, double* u_in, int64_t dim_in, do
   if (nst < 1 || nsd < nst || nsd > MAXS || dim_in < N || prm->davidson_sze_max < 1 ||
       (prm->precision != QPGPU_FP64 && prm->precision != QPGPU_FP32 && prm->precision != QPGPU_FF))
     return qpgpu_fail(c, QPGPU_ERR_ARG, "bad Davidson parameters (1 <= n_states <= n_states_diag <= 8)");
-  if (prm->algebra != QPGPU_ALGEBRA_FAST && prm->algebra != QPGPU_ALGEBRA_FP64)
-    return qpgpu_fail(c, QPGPU_ERR_ARG, "algebra must be QPGPU_ALGEBRA_FAST or QPGPU_ALGEBRA_FP64");
+  if (prm->algebra != QPGPU_ALGEBRA_FAST && prm->algebra != QPGPU_ALGEBRA_FP64 && prm->algebra != QPGPU_ALGEBRA_TC)
+    return qpgpu_fail(c, QPGPU_ERR_ARG, "algebra must be QPGPU_ALGEBRA_FAST, _FP64 or _TC");
   if (prm->dressed && !c->dress.on) return qpgpu_fail(c, QPGPU_ERR_STATE, "dressed Davidson without a dressing");
   if (prm->preconditioner < 0 || prm->preconditioner > 2)
     return qpgpu_fail(c, QPGPU_ERR_ARG, "preconditioner must be 0 (diagonal), 1 (learned) or 2 (learned, extra direction)");
@@ -1318,6 +1366,8 @@ extern "C" int qpgpu_davidson_hs2(qpgpu_ctx* c, double* u_in, int64_t dim_in, do
   // tall-skinny algebra of the mixed modes on the FP32 pipes (float-float /
   // FP32), or in FP64 like the plain loop (algebra = QPGPU_ALGEBRA_FP64)
   const bool ffalg = mixed && prm->algebra == QPGPU_ALGEBRA_FAST;
+  // FP64-accurate Gram blocks on the tensor cores (any precision)
+  const bool tcalg = prm->algebra == QPGPU_ALGEBRA_TC;
   const int restart_prec = prm->precision == QPGPU_FF ? QPGPU_FF : QPGPU_FP64;  // defect-correction sigma
   if (mixed && prm->defect_every > 0) itermax = std::max(3, std::min(itermax, prm->defect_every + 1));
   const int max_sigma = prm->max_iter > 0 ? prm->max_iter : 1000;
@@ -1331,6 +1381,7 @@ extern "C" int qpgpu_davidson_hs2(qpgpu_ctx* c, double* u_in, int64_t dim_in, do
   d.nst = nst;
   d.itermax = itermax;
   d.ncta = 2 * c->n_sm;  // two CTAs per SM
+  d.tc = tcalg;
   d.rows_per_cta = (N + d.ncta - 1) / d.ncta;
   const size_t blkn = (size_t)N * nsd;
   if (dev_alloc(&d.U, blkn * itermax) != cudaSuccess || dev_alloc(&d.W, blkn * itermax) != cudaSuccess ||
@@ -1339,6 +1390,14 @@ extern "C" int qpgpu_davidson_hs2(qpgpu_ctx* c, double* u_in, int64_t dim_in, do
       dev_alloc(&d.small, (size_t)SMALL_DOUBLES) != cudaSuccess) {
     cudaGetLastError();
     return qpgpu_fail(c, QPGPU_ERR_NOMEM, "Davidson work arrays do not fit on the device");
+  }
+  if (tcalg) {
+    if (qp_gram_oz_prepare() || dev_alloc(&d.uexp, MAXM) != cudaSuccess ||
+        dev_alloc(&d.bexp, 2 * MAXS + 1) != cudaSuccess) {
+      cudaGetLastError();
+      return qpgpu_fail(c, QPGPU_ERR_NOMEM, "tensor-core Gram work arrays could not be set up");
+    }
+    QP_CUDA(c, cudaMemsetAsync(d.bexp, 0, (2 * MAXS + 1) * sizeof(int), d.st));
   }
   d.sUf = (int64_t)blkn;
   if (ffalg && (dev_alloc(&d.Uf, blkn * itermax) != cudaSuccess || dev_alloc(&d.Bf, blkn * 2) != cudaSuccess)) {
@@ -1449,6 +1508,8 @@ extern "C" int qpgpu_davidson_hs2(qpgpu_ctx* c, double* u_in, int64_t dim_in, do
       if (ffalg) {
         split_block(d, d.blk(d.W, b), d.blk(d.S, b), d.Bf);
         gram_ff(d, d.Uf, shift2, d.Bf, 2 * nsd, d.small + OFF_X);
+      } else if (tcalg) {
+        gram_tc(d, d.U, shift2, d.blk(d.W, b), d.blk(d.S, b), d.small + OFF_X, TC_BASIS);
       } else {
         gram(d, d.U, shift2, d.blk(d.W, b), d.blk(d.S, b), d.small + OFF_X);
       }
@@ -1538,7 +1599,7 @@ extern "C" int qpgpu_davidson_hs2(qpgpu_ctx* c, double* u_in, int64_t dim_in, do
       double* ydev = d.small + OFF_Y;
       prof.mark(DavProf::HOST);
       QP_CUDA(c, cudaMemcpyAsync(ydev, ycoef.data(), ycoef.size() * sizeof(double), cudaMemcpyHostToDevice, st));
-      if (ffalg && prec == QPGPU_FP32)  // W, S from the FP32 sigma: Ritz vectors in FP32, they only feed the step
+      if ((ffalg || tcalg) && prec == QPGPU_FP32)  // W, S from the FP32 sigma: FP32 Ritz vectors feed the step
         lincomb32(d, shift2, ydev, d.U, d.blk(d.U, iter), d.W, d.blk(d.W, iter), d.S, d.blk(d.S, iter));
       else if (ffalg)  // restart iteration: float-float
         lincomb_ff(d, shift2, ydev, d.U, d.blk(d.U, iter), d.W, d.blk(d.W, iter), d.S, d.blk(d.S, iter));
@@ -1577,7 +1638,14 @@ extern "C" int qpgpu_davidson_hs2(qpgpu_ctx* c, double* u_in, int64_t dim_in, do
         k_step<<<d.ncta, DBLK, 0, st>>>(d.blk(d.U, iter), d.blk(d.W, iter), d.blk(d.S, iter), hjj, N, sp, d.part);
       QP_CUDA(c, cudaGetLastError());
       QP_CUDA(c, cudaMemcpyAsync(partial.data(), d.part, partial.size() * sizeof(double), cudaMemcpyDeviceToHost, st));
+      int tc_status = 0;
+      if (tcalg)
+        QP_CUDA(c, cudaMemcpyAsync(&tc_status, d.bexp + 2 * MAXS, sizeof(int), cudaMemcpyDeviceToHost, st));
       QP_CUDA(c, cudaStreamSynchronize(st));
+      if (tc_status) {
+        cudaEventDestroy(ev0);
+        return qpgpu_fail(c, QPGPU_ERR_TIMEOUT, "Davidson: a bounded tensor-core wait of the Gram blocks ran out");
+      }
       prof.mark(DavProf::STEP);
       double mx = 0.0;
       for (int k = 0; k < nst; ++k) {

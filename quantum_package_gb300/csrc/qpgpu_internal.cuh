@@ -443,6 +443,8 @@ struct qpgpu_ctx {
   std::vector<std::pair<std::string, cudaEvent_t>> marks;
 
   int* d_flag = nullptr;  // NaN / Inf flag of the host-array entry points
+  void* d_tc_scratch = nullptr;  // qpgpu_gram_tc: per-CTA partials, exponents, status
+  size_t tc_scratch_bytes = 0;
   // scratch for the host-pointer sigma entry points
   double* d_work = nullptr;
   size_t work_bytes = 0;
@@ -511,6 +513,15 @@ void qp_report_marks(qpgpu_ctx* c);  // ctx.cu
 // v, s of u (nst states fastest); no-op without a dressing
 int qp_dress(qpgpu_ctx* c, double* v, double* s, const double* u, int nst, cudaStream_t st);
 void qp_free_dressing(qpgpu_ctx* c);
+
+// FP64-accurate Gram blocks on the tensor cores (ozaki.cu)
+int qp_gram_oz_prepare();
+void qp_col_maxexp(const double* X, int nblk, int64_t sX, int nsd, int ld, int64_t N, int* E, int col0,
+                   const int* skip, cudaStream_t st, int n_sm);
+void qp_gram_oz(const double* A, int64_t sA, int m, int nsdA, int ldA, const double* B0, const double* B1, int nbc,
+                int nsdB, int ldB, int64_t N, const int* eA, const int* eB, double* partial, int ncta,
+                const int* skip, int* status, cudaStream_t st);
+void qp_oz_reduce(const double* partial, int ncta, int np, double* out, const int* skip, cudaStream_t st);
 
 // learned preconditioner (mlp.cu)
 int qp_det_features(qpgpu_ctx* c);

@@ -90,17 +90,20 @@ def test_davidson_mixed_tight(prec_name, nsd, nst):
 
 
 @pytest.mark.parametrize("threshold,tol", [(1e-10, 1e-6), (1e-12, 1e-9)])
-def test_davidson_mixed_fp64_algebra(threshold, tol):
-    # FP32 sigma with the FP64 sigma at each restart, every other operation
-    # (projections, Gram-Schmidt, Ritz vectors, step, residual norms) in FP64
-    from quantum_package_gb300 import ALGEBRA_FP64
+@pytest.mark.parametrize("algebra_name", ["FP64", "TC"])
+def test_davidson_mixed_fp64_algebra(threshold, tol, algebra_name):
+    # FP32 sigma with the FP64 sigma at each restart; projections,
+    # Gram-Schmidt, step and residual norms in FP64 -- on the FP64 pipe, or
+    # with the Gram blocks FP64-accurate on the tensor cores (TC)
+    from quantum_package_gb300 import ALGEBRA_FP64, ALGEBRA_TC
     from quantum_package_gb300.sigma import Wavefunction
+    algebra = {"FP64": ALGEBRA_FP64, "TC": ALGEBRA_TC}[algebra_name]
     p = G.make_problem(2, n_det=20_000, n_states=4)
     wf = Wavefunction.from_problem(p)
     u = _guess(p.n_det, 8, 3)
     kw = dict(n_states=4, threshold=threshold, s2_eig=False, max_iter=500)
     r64 = wf.davidson_diag_hs2(u, **kw)
-    rs = wf.davidson_diag_hs2(u, precision=FP32, algebra=ALGEBRA_FP64, **kw)
+    rs = wf.davidson_diag_hs2(u, precision=FP32, algebra=algebra, **kw)
     assert r64["converged"] and rs["converged"]
     np.testing.assert_allclose(rs["energies"][:4], r64["energies"][:4], rtol=0, atol=tol)
     tr = rs["trace"]
@@ -123,3 +126,18 @@ def test_davidson_state_following_matches_oracle():
     r = wf.davidson_diag_hs2(u, n_states=2, davidson_sze_max=8, state_following=True, max_iter=300, **kw)
     assert r["converged"]
     np.testing.assert_allclose(r["energies"][:2], eo[:2], rtol=0, atol=1e-8)
+
+
+def test_davidson_fp64_with_tensor_core_grams_matches_oracle():
+    # plain FP64 sigma with the Gram blocks on the tensor cores: the same
+    # energies as the oracle's CPU Davidson
+    from quantum_package_gb300 import ALGEBRA_TC
+    from quantum_package_gb300.sigma import Wavefunction
+    p = G.make_problem(1, n_det=3000)
+    wf = Wavefunction.from_problem(p)
+    o = Oracle.from_problem(p)
+    u = _guess(p.n_det, 4, 11)
+    r = wf.davidson_diag_hs2(u, n_states=2, threshold=1e-12, s2_eig=False, max_iter=300, algebra=ALGEBRA_TC)
+    eo, _, _, _, _ = o.davidson(u, 2, threshold=1e-12, s2_eig=False, max_sigma=300)
+    assert r["converged"]
+    np.testing.assert_allclose(r["energies"][:2], eo[:2], rtol=0, atol=1e-9)
