@@ -10,7 +10,9 @@
 // for every element (k_col_maxexp).  An element is rounded to the 56-bit
 // fixed-point integer F = round(|x| 2^(56 - E_c)) and written in balanced
 // base 128, F = sum_p d_p 2^(49 - 7p) with d_1..d_7 in [-64, 63] and d_0 in
-// [0, 128], every digit times the sign of x: integers exact in BF16.
+// [0, 128], every digit times the sign of x: integers exact in BF16.  The
+// digits are those of F + 64 (1 + 2^7 + ... + 2^49) less 64 each, so they
+// come out of independent shifts and masks, with no carry chain.
 // Balanced digits make both the rounding and the dropped low-order products
 // zero-mean, so they do not pile up in sums of squares (Gram diagonals).
 //
@@ -27,46 +29,60 @@
 // becomes an FP64 value and the CTAs are summed in FP64 in a fixed order.
 //
 // Pipeline (one CTA per SM over a contiguous block of rows, chunks of 32
-// rows).  Warps 0-7 split: the raw FP64 rows of chunk c + 1 stream into
-// shared memory with cp.async while chunk c is cut into digit planes (16-byte
-// stores of 8 rows of one column), then they arrive on full[s].  Warp 8
-// issues the chunk's 36 x 2 MMAs once full[s] completes and commits them to
-// empty[s] (the stage may be overwritten) and, at the end of a window, to
-// accf[b]; the window's accumulators alternate between two tensor-memory
-// buffers b.  Warps 0-3, whose lane quarters cover the 128 accumulator rows,
-// flush a finished window and arrive on acce[b] before warp 8 reuses b.
-// Every mbarrier wait is bounded: one that runs out sets the CTA's error
-// flag, the warps finish their loops without further work, the kernel waits
-// (bounded) for its MMAs and frees its tensor memory, and *status is set.
+// rows), one role per warp:
+//  * warp 13 streams the raw FP64 rows of each chunk into a ring of raw
+//    stages (cp.async.bulk per operand block, completing on rawfull[r]; a
+//    block whose rows are strided or unaligned is copied by the warp's lanes);
+//  * warps 0-7 cut the chunk into digit planes (stores of 2, 4 or 8 rows of
+//    one column), free the raw stage (rawempty[r]) and fill digit stage s
+//    (full[s]);
+//  * warp 12 issues the chunk's 16 MMAs once full[s] completes and commits
+//    them to empty[s] and, at the end of a window, to accf[b]; the windows
+//    rotate over four tensor-memory accumulator buffers b;
+//  * warps 8-11, whose lane quarters cover the 128 accumulator rows, add a
+//    finished window to their int64 sums and arrive on acce[b], so that the
+//    integer work never holds up the splitting.
+// A plane p of A meets B planes 0..7-p only (levels p..7), so its MMA has
+// N = (8 - p) 16 and writes the accumulator from level p on.
+// Every mbarrier wait is bounded and gives up early once another warp has set
+// the CTA's error flag; the warps then leave their loops, the kernel waits
+// (bounded) for its bulk copies and MMAs, frees its tensor memory and sets
+// *status.
 #include <algorithm>
 
 #include "qpgpu_internal.cuh"
 
 namespace {
 
-constexpr int OZ_SPLIT = 256;               // splitting threads (warps 0-7)
-constexpr int OZ_THREADS = OZ_SPLIT + 32;   // + the MMA warp (warp 8)
-constexpr int OZ_M = 128;                   // MMA M: columns of A (padded)
-constexpr int OZ_N = 16;                    // MMA N: columns of B (padded)
-constexpr int OZ_KC = 32;                   // rows per chunk (MMA K = 2 x 16)
-constexpr int OZ_DIG = 8;                   // digit planes per operand
-constexpr int OZ_LEVELS = 8;                // levels p + q = 0..7 kept
-constexpr int OZ_WINDOW = 4;                // chunks per accumulator window (128 rows)
+constexpr int OZ_SPLIT = 256;                // splitting threads (warps 0-7)
+constexpr int OZ_FLUSH_WARP = 8;             // warps 8-11 flush the accumulators
+constexpr int OZ_MMA_WARP = 12;              // issues the MMAs, owns the tensor memory
+constexpr int OZ_LOAD_WARP = 13;             // streams the raw rows
+constexpr int OZ_THREADS = 14 * 32;
+constexpr int OZ_M = 128;                    // MMA M: columns of A (padded)
+constexpr int OZ_N = 16;                     // columns of B (padded)
+constexpr int OZ_KC = 32;                    // rows per chunk (MMA K = 2 x 16)
+constexpr int OZ_DIG = 8;                    // digit planes per operand
+constexpr int OZ_LEVELS = 8;                 // levels p + q = 0..7 kept
+constexpr int OZ_WINDOW = 4;                 // chunks per accumulator window (128 rows)
+constexpr int OZ_NBUF = 4;                   // accumulator buffers
 constexpr int OZ_A_TILE = OZ_M * OZ_KC * 2;  // bytes of one A digit plane
 constexpr int OZ_B_TILE = OZ_N * OZ_KC * 2;
-constexpr int OZ_NMMA = OZ_LEVELS * OZ_N;   // MMA N: the 8 levels of the 16 columns of B
-// a stage: the 8 A planes, then 7 zero B tiles and the 8 B planes, so that the
-// B operand of A plane p (B planes L - p for levels L = 0..7, zero where
-// L < p) is the 128-row window starting at tile 7 - p
-constexpr int OZ_STAGE = OZ_DIG * OZ_A_TILE + (OZ_DIG - 1 + OZ_DIG) * OZ_B_TILE;
+// a digit stage: the 8 A planes, then the 8 B planes, so that B planes
+// 0..n-1 form one K-major operand of 16 n rows
+constexpr int OZ_STAGE = OZ_DIG * OZ_A_TILE + OZ_DIG * OZ_B_TILE;
 constexpr int OZ_TAB = 6144;  // alignment, exponents, block tables, barriers
 constexpr int OZ_SMEM_MAX = 232448;
 constexpr int OZ_MAXRAW = 8;  // raw stages at most
 constexpr int OZ_MAXBLK = OZ_M + 2;  // operand blocks: at most one per column of A, two of B
 
-constexpr int OZ_ACC_COLS = OZ_LEVELS * OZ_N;  // 128 tensor-memory columns per buffer
-constexpr int OZ_TMEM_COLS = 2 * OZ_ACC_COLS;  // two buffers
+constexpr int OZ_ACC_COLS = OZ_LEVELS * OZ_N;     // 128 tensor-memory columns per buffer
+constexpr int OZ_TMEM_COLS = OZ_NBUF * OZ_ACC_COLS;  // 512: the whole tensor memory of the SM
 constexpr long long OZ_WAIT_LIMIT = 1LL << 25;
+
+// barrier slots
+constexpr int OZ_B_FULL = 0, OZ_B_EMPTY = 2, OZ_B_ACCF = 4, OZ_B_ACCE = OZ_B_ACCF + OZ_NBUF,
+              OZ_B_RAWF = OZ_B_ACCE + OZ_NBUF, OZ_B_RAWE = OZ_B_RAWF + OZ_MAXRAW, OZ_NBARS = OZ_B_RAWE + OZ_MAXRAW;
 
 struct OzArgs {
   const double* A;  // blocks of nsdA columns, rows ldA values apart, blocks sA apart
@@ -81,8 +97,9 @@ struct OzArgs {
   double* partial;  // [cta][m][nbc]
   const int* skip;
   int* status;
-  int nraw;        // raw stages in the ring (chunks c + 1 .. c + nraw - 1 stream in during the split of c)
+  int nraw;        // raw stages in the ring
   int raw_stride;  // doubles per raw stage
+  int rpt;         // rows per splitting task: 2, 4 or 8
 };
 
 __device__ __forceinline__ uint32_t smem_u32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
@@ -104,56 +121,42 @@ __device__ __forceinline__ uint64_t sdesc(uint32_t addr) {
 
 // instruction descriptor of kind::f16: FP32 accumulator, BF16 A and B, both
 // K-major, N >> 3 at bit 17, M >> 4 at bit 24
-constexpr uint32_t OZ_IDESC = (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(OZ_NMMA >> 3) << 17) |
-                              ((uint32_t)(OZ_M >> 4) << 24);
-
-// rint(v / 128) (round to nearest even) through the 1.5 * 2^23 constant;
-// v / 128 is exact and the one rounding of the FMA is the wanted one (|v| < 2^29)
-__device__ __forceinline__ float oz_rint128(float v) {
-  return __fsub_rn(__fmaf_rn(v, 0.0078125f, 12582912.0f), 12582912.0f);
+__device__ __forceinline__ uint32_t oz_idesc(int n) {
+  return (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(n >> 3) << 17) | ((uint32_t)(OZ_M >> 4) << 24);
 }
+
+// 64 in every base-128 digit position of a 56-bit integer
+constexpr unsigned long long OZ_H = 64ull * ((1ull << 49) | (1ull << 42) | (1ull << 35) | (1ull << 28) |
+                                             (1ull << 21) | (1ull << 14) | (1ull << 7) | 1ull);
 
 // the 8 balanced digits of x against the column's biased max exponent eb
 // (|x| < 2^(eb - 1022)), as FP32 values (exact small integers, so their top
-// 16 bits are their BF16 bits).  F = round(|x| 2^(56 - E)), E = eb - 1022, is
-// cut into three integer pieces of 14, 21 and 21 bits, each exact in FP32
-// (with the sign of x); a digit is then v - 128 rint(v / 128) and the
-// quotient carries into the next piece, all exact FP32 operations.
+// 16 bits are their BF16 bits).  F = round(|x| 2^(56 - E)), E = eb - 1022,
+// is the 53-bit significand M = m53 2^3 rounded-shifted right by eb - ex
+// (<= 2^56).  With G = F + OZ_H, the plain base-128 digits g_p of G less 64
+// are a balanced expansion of F: F = sum_p (g_p - 64) 2^(49 - 7p), d_0 in
+// [0, 128] and d_1..d_7 in [-64, 63].  No digit waits on another: each is a
+// shift, a mask with the 2^23 exponent bits, and one exact FMA that removes
+// 2^23 + 64 and applies the sign of x.
 __device__ __forceinline__ void oz_digits(double x, int eb, float (&d)[OZ_DIG]) {
   const unsigned long long b = (unsigned long long)__double_as_longlong(x);
-  const int ex = (int)((b >> 52) & 0x7FF);
+  const uint32_t bh = (uint32_t)(b >> 32);
+  const int ex = (int)((bh >> 20) & 0x7FF);
+  const int k = max(eb - ex, 0);
   unsigned long long F = 0;
-  if (ex != 0) {
-    const unsigned long long m53 = (b & 0xFFFFFFFFFFFFFull) | (1ull << 52);
-    // x = m53 2^(ex - 1075), so F = m53 2^(ex - eb + 3); the shift is <= 3
-    const int sh = ex - eb + 3;
-    if (sh >= 0)
-      F = m53 << sh;
-    else if (sh > -55)
-      F = (m53 + (1ull << (-sh - 1))) >> (-sh);
+  if (ex != 0 && k < 57) {
+    const unsigned long long M = ((b & 0xFFFFFFFFFFFFFull) | (1ull << 52)) << 3;
+    F = k == 0 ? M : (M + (1ull << (k - 1))) >> k;
   }
-  const float sgn = ((long long)b < 0) ? -1.0f : 1.0f;
-  const float P2 = sgn * __fsub_rn(__uint_as_float(0x4B000000u | ((uint32_t)F & 0x1FFFFFu)), 8388608.0f);
-  float P1 = sgn * __fsub_rn(__uint_as_float(0x4B000000u | ((uint32_t)(F >> 21) & 0x1FFFFFu)), 8388608.0f);
-  float P0 = sgn * __fsub_rn(__uint_as_float(0x4B000000u | (uint32_t)(F >> 42)), 8388608.0f);
-  float v = P2;
+  const unsigned long long G = F + OZ_H;
+  const uint32_t gl = (uint32_t)G, gh = (uint32_t)(G >> 32);
+  const uint32_t sbit = bh & 0x80000000u;
+  const float sg = __uint_as_float(sbit | 0x3F800000u);   // +-1
+  const float sc = __uint_as_float(sbit | 0x4B000040u);   // +-(2^23 + 64)
+  const uint32_t g[OZ_DIG] = {gh >> 17, gh >> 10, gh >> 3, __funnelshift_r(gl, gh, 28), gl >> 21, gl >> 14, gl >> 7, gl};
 #pragma unroll
-  for (int p = 7; p >= 5; --p) {
-    const float q = oz_rint128(v);
-    d[p] = __fmaf_rn(-q, 128.0f, v);
-    v = q;
-  }
-  v = __fadd_rn(P1, v);
-#pragma unroll
-  for (int p = 4; p >= 2; --p) {
-    const float q = oz_rint128(v);
-    d[p] = __fmaf_rn(-q, 128.0f, v);
-    v = q;
-  }
-  v = __fadd_rn(P0, v);
-  const float q = oz_rint128(v);
-  d[1] = __fmaf_rn(-q, 128.0f, v);
-  d[0] = q;
+  for (int p = 0; p < OZ_DIG; ++p)
+    d[p] = __fmaf_rn(sg, __uint_as_float(0x4B000000u | (g[p] & (p == 0 ? 0xFFu : 0x7Fu))), -sc);
 }
 
 // BF16 bits of two exact small-integer FP32 values, packed (lo, hi)
@@ -161,17 +164,30 @@ __device__ __forceinline__ uint32_t bf16x2(float lo, float hi) {
   return __byte_perm(__float_as_uint(lo), __float_as_uint(hi), 0x7632);
 }
 
-// bounded wait for the completion of phase `parity` of an mbarrier
-__device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity) {
+__device__ __forceinline__ bool mbar_try(uint32_t bar, uint32_t parity) {
+  uint32_t done;
+  asm volatile(
+      "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}"
+      : "=r"(done)
+      : "r"(bar), "r"(parity)
+      : "memory");
+  return done != 0;
+}
+
+// bounded wait for the completion of phase `parity` of an mbarrier; gives up
+// early once the CTA's error flag is set
+__device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity, const int* sflag) {
   for (long long it = 0; it < OZ_WAIT_LIMIT; ++it) {
-    uint32_t done;
-    asm volatile(
-        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}"
-        : "=r"(done)
-        : "r"(bar), "r"(parity)
-        : "memory");
-    if (done) return true;
+    if (mbar_try(bar, parity)) return true;
+    if ((it & 255) == 255 && *(volatile const int*)sflag) return false;
   }
+  return false;
+}
+
+// bounded wait that ignores the error flag: for the drains before exit
+__device__ __forceinline__ bool mbar_drain(uint32_t bar, uint32_t parity) {
+  for (long long it = 0; it < OZ_WAIT_LIMIT; ++it)
+    if (mbar_try(bar, parity)) return true;
   return false;
 }
 
@@ -183,26 +199,61 @@ __device__ __forceinline__ void mma_commit(uint32_t bar) {
   asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(bar) : "memory");
 }
 
-// adds level L of accumulator buffer `buf` (this warp's 32 lanes, 16
-// columns), each an exact integer below 2^23, shifted by sh, to acc
-__device__ __forceinline__ void oz_flush_level(uint32_t tmem, int warp, int buf, int L, int sh,
-                                               long long (&acc)[OZ_N]) {
+// level L of accumulator buffer `buf` (this warp's 32 lanes, 16 columns),
+// exact integers below 2^23, shifted by sh into acc
+__device__ __forceinline__ void oz_flush1(uint32_t taddr, int sh, long long (&acc)[OZ_N]) {
   uint32_t v[16];
   asm volatile(
       "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
       : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]), "=r"(v[4]), "=r"(v[5]), "=r"(v[6]), "=r"(v[7]), "=r"(v[8]),
         "=r"(v[9]), "=r"(v[10]), "=r"(v[11]), "=r"(v[12]), "=r"(v[13]), "=r"(v[14]), "=r"(v[15])
-      : "r"(tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)(buf * OZ_ACC_COLS + L * OZ_N)));
+      : "r"(taddr));
   asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
 #pragma unroll
-  for (int j = 0; j < OZ_N; ++j) acc[j] += (long long)__float2ll_rz(__uint_as_float(v[j])) << sh;
+  for (int j = 0; j < OZ_N; ++j) acc[j] += (long long)__float2int_rn(__uint_as_float(v[j])) << sh;
+}
+
+// digit planes of one chunk: task (column, group of RPT rows) writes RPT
+// rows of one column into each of the 8 planes of stage (sa, sb)
+template <int RPT>
+__device__ __forceinline__ void oz_split(const double* rsrc, uint8_t* sa, uint8_t* sb, int m, int rw, int nrow,
+                                         const int* coff, const int* cw, const int* sE, int tid) {
+  const int ntask = rw * (OZ_KC / RPT);
+  for (int t = tid; t < ntask; t += OZ_SPLIT) {
+    const int grp = t / rw, col = t - grp * rw;
+    const bool isA = col < m;
+    const int cc = isA ? col : col - m;
+    const int eb = sE[isA ? cc : OZ_M + cc];
+    const int wcol = cw[col], k0 = RPT * grp;
+    const double* xs = rsrc + coff[col] + k0 * wcol;
+    uint32_t pk[OZ_DIG][RPT / 2];
+#pragma unroll
+    for (int k = 0; k < RPT; k += 2) {
+      float d0[OZ_DIG], d1[OZ_DIG];
+      oz_digits(k0 + k < nrow ? xs[k * wcol] : 0.0, eb, d0);
+      oz_digits(k0 + k + 1 < nrow ? xs[(k + 1) * wcol] : 0.0, eb, d1);
+#pragma unroll
+      for (int p = 0; p < OZ_DIG; ++p) pk[p][k >> 1] = bf16x2(d0[p], d1[p]);
+    }
+    uint8_t* dst = (isA ? sa : sb) + kmaj(cc, k0);
+    const int tile = isA ? OZ_A_TILE : OZ_B_TILE;
+#pragma unroll
+    for (int p = 0; p < OZ_DIG; ++p) {
+      if constexpr (RPT == 8)
+        *reinterpret_cast<uint4*>(dst + p * tile) = make_uint4(pk[p][0], pk[p][1], pk[p][2], pk[p][3]);
+      else if constexpr (RPT == 4)
+        *reinterpret_cast<uint2*>(dst + p * tile) = make_uint2(pk[p][0], pk[p][1]);
+      else
+        *reinterpret_cast<uint32_t*>(dst + p * tile) = pk[p][0];
+    }
+  }
 }
 
 __global__ void __launch_bounds__(OZ_THREADS, 1) k_gram_oz(OzArgs g) {
   if (g.skip && *g.skip) return;
   extern __shared__ __align__(1024) uint8_t smem[];
   uint8_t* sbase = (uint8_t*)(((uintptr_t)smem + 1023) & ~(uintptr_t)1023);
-  uint8_t* tiles = sbase;                                 // stage s: A planes, then B planes
+  uint8_t* tiles = sbase;                                 // digit stage s: A planes, then B planes
   double* raw = (double*)(sbase + 2 * OZ_STAGE);          // nraw stages, operand blocks of [OZ_KC][width]
   const double** bsrc = (const double**)(sbase + 2 * OZ_STAGE + (size_t)g.nraw * g.raw_stride * 8);  // block bases
   int* bw = (int*)(bsrc + OZ_MAXBLK);                     // [OZ_MAXBLK] block widths
@@ -212,31 +263,35 @@ __global__ void __launch_bounds__(OZ_THREADS, 1) k_gram_oz(OzArgs g) {
   int* cw = coff + OZ_M + OZ_N;                           // [OZ_M + OZ_N] width of its block
   int* sE = cw + OZ_M + OZ_N;                             // [OZ_M] A, [OZ_N] B exponents
   uint64_t* bars = (uint64_t*)(((uintptr_t)(sE + OZ_M + OZ_N) + 7) & ~(uintptr_t)7);
-  // full[2], empty[2], accf[2], acce[2], rawbar[OZ_MAXRAW]
-  uint32_t* tmem_slot = (uint32_t*)(bars + 8 + OZ_MAXRAW);
+  uint32_t* tmem_slot = (uint32_t*)(bars + OZ_NBARS);
   int* sflag = (int*)(tmem_slot + 1);                     // error flag of the CTA
   int* snblk = sflag + 1;
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   const int m = g.m, nbc = g.nbc, rw = m + nbc;
-  const uint32_t full0 = smem_u32(&bars[0]), empty0 = smem_u32(&bars[2]);
-  const uint32_t accf0 = smem_u32(&bars[4]), acce0 = smem_u32(&bars[6]), rawb0 = smem_u32(&bars[8]);
+  const uint32_t bar0 = smem_u32(bars);
+  auto BAR = [&](int slot, int i) { return bar0 + 8u * (uint32_t)(slot + i); };
 
   for (int i = tid; i < 2 * OZ_STAGE / 16; i += OZ_THREADS) reinterpret_cast<uint4*>(tiles)[i] = make_uint4(0, 0, 0, 0);
   for (int i = tid; i < OZ_M; i += OZ_THREADS) sE[i] = i < m ? g.eA[i] : 0;
   for (int j = tid; j < OZ_N; j += OZ_THREADS) sE[OZ_M + j] = j < nbc ? g.eB[j] : 0;
-  if (warp == 8) {
+  if (warp == OZ_MMA_WARP) {
     asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(tmem_slot)),
                  "r"(OZ_TMEM_COLS));
     asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
   }
   if (tid == 0) {
     for (int s = 0; s < 2; ++s) {
-      asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(full0 + 8 * s), "r"(OZ_SPLIT));
-      asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(empty0 + 8 * s));
-      asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(accf0 + 8 * s));
-      asm volatile("mbarrier.init.shared::cta.b64 [%0], 128;" ::"r"(acce0 + 8 * s));
+      asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(BAR(OZ_B_FULL, s)), "r"(OZ_SPLIT / 32));
+      asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(BAR(OZ_B_EMPTY, s)));
     }
-    for (int s = 0; s < OZ_MAXRAW; ++s) asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(rawb0 + 8 * s));
+    for (int b = 0; b < OZ_NBUF; ++b) {
+      asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(BAR(OZ_B_ACCF, b)));
+      asm volatile("mbarrier.init.shared::cta.b64 [%0], 4;" ::"r"(BAR(OZ_B_ACCE, b)));
+    }
+    for (int r = 0; r < OZ_MAXRAW; ++r) {
+      asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(BAR(OZ_B_RAWF, r)));
+      asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(BAR(OZ_B_RAWE, r)), "r"(OZ_SPLIT / 32));
+    }
     asm volatile("fence.mbarrier_init.release.cluster;");
     *sflag = 0;
     // operand blocks: A in blocks of nsdA columns, then B0 and B1; each is
@@ -277,32 +332,136 @@ __global__ void __launch_bounds__(OZ_THREADS, 1) k_gram_oz(OzArgs g) {
   const int64_t r1 = min(r0 + g.rows_per_cta, g.N);
   const int nchunks = r1 > r0 ? (int)((r1 - r0 + OZ_KC - 1) / OZ_KC) : 0;
   const int nwin = (nchunks + OZ_WINDOW - 1) / OZ_WINDOW;
-  long long hi[OZ_N], lo[OZ_N];  // fixed-point sums of this thread's A column (warps 0-3)
+  const int nraw = g.nraw;
+  long long hi[OZ_N], lo[OZ_N];  // fixed-point sums of this thread's A column (flush warps)
 #pragma unroll
   for (int j = 0; j < OZ_N; ++j) hi[j] = lo[j] = 0;
 
-  if (warp < 8) {
+  if (warp < OZ_SPLIT / 32) {
     // ---- splitting warps -------------------------------------------------
+    for (int c = 0; c < nchunks; ++c) {
+      const int s = c & 1, rs = c % nraw;
+      // chunk c's raw rows have landed; the MMAs of chunk c - 2 are done with digit stage s
+      bool ok = mbar_wait(BAR(OZ_B_RAWF, rs), (uint32_t)(c / nraw) & 1u, sflag);
+      if (ok && c >= 2) ok = mbar_wait(BAR(OZ_B_EMPTY, s), (uint32_t)((c >> 1) - 1) & 1u, sflag);
+      if (!__all_sync(0xffffffffu, ok)) {
+        if (lane == 0) atomicExch(sflag, 1);
+        break;
+      }
+      uint8_t* sa = tiles + s * OZ_STAGE;
+      uint8_t* sb = sa + OZ_DIG * OZ_A_TILE;
+      const double* rsrc = raw + (size_t)rs * g.raw_stride;
+      const int nrow = (int)min((int64_t)OZ_KC, r1 - (r0 + (int64_t)c * OZ_KC));
+      if (g.rpt == 8)
+        oz_split<8>(rsrc, sa, sb, m, rw, nrow, coff, cw, sE, tid);
+      else if (g.rpt == 4)
+        oz_split<4>(rsrc, sa, sb, m, rw, nrow, coff, cw, sE, tid);
+      else
+        oz_split<2>(rsrc, sa, sb, m, rw, nrow, coff, cw, sE, tid);
+      asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+      __syncwarp();
+      if (lane == 0) {
+        mbar_arrive(BAR(OZ_B_RAWE, rs));
+        mbar_arrive(BAR(OZ_B_FULL, s));
+      }
+    }
+  } else if (warp < OZ_MMA_WARP) {
+    // ---- flush warps: lane quarter q = warp % 4 holds rows 32 q .. 32 q + 31
+    const uint32_t lrow = (uint32_t)((warp & 3) * 32) << 16;
+    for (int w = 0; w < nwin; ++w) {
+      const int buf = w % OZ_NBUF;
+      const bool ok = mbar_wait(BAR(OZ_B_ACCF, buf), (uint32_t)(w / OZ_NBUF) & 1u, sflag);
+      if (!__all_sync(0xffffffffu, ok)) {
+        if (lane == 0) atomicExch(sflag, 1);
+        break;
+      }
+      asm volatile("tcgen05.fence::after_thread_sync;");
+      const uint32_t ta = tmem + lrow + (uint32_t)(buf * OZ_ACC_COLS);
+#pragma unroll
+      for (int L = 0; L < OZ_LEVELS / 2; ++L) oz_flush1(ta + L * OZ_N, 7 * (3 - L), hi);
+#pragma unroll
+      for (int L = OZ_LEVELS / 2; L < OZ_LEVELS; ++L) oz_flush1(ta + L * OZ_N, 7 * (7 - L), lo);
+      asm volatile("tcgen05.fence::before_thread_sync;");
+      __syncwarp();
+      if (lane == 0) mbar_arrive(BAR(OZ_B_ACCE, buf));
+    }
+  } else if (warp == OZ_MMA_WARP) {
+    // ---- MMA warp: lane 0 issues, the warp stays converged ----------------
+    uint32_t last_bar = 0, last_par = 0;  // the latest commit: its completion covers every MMA
+    for (int c = 0; c < nchunks; ++c) {
+      const int s = c & 1, w = c / OZ_WINDOW, buf = w % OZ_NBUF;
+      bool ok = true;
+      if (lane == 0) {
+        // accumulator buffer flushed (window w - 4), digit stage s full
+        if (c % OZ_WINDOW == 0 && w >= OZ_NBUF)
+          ok = mbar_wait(BAR(OZ_B_ACCE, buf), (uint32_t)(w / OZ_NBUF - 1) & 1u, sflag);
+        if (ok) ok = mbar_wait(BAR(OZ_B_FULL, s), (uint32_t)(c >> 1) & 1u, sflag);
+        if (ok) {
+          asm volatile("tcgen05.fence::after_thread_sync;");
+          const bool first = (c % OZ_WINDOW) == 0;
+          const uint32_t a0 = smem_u32(tiles + s * OZ_STAGE);
+          const uint32_t b0 = a0 + OZ_DIG * OZ_A_TILE;  // B planes 0..7
+#pragma unroll
+          for (int p = 0; p < OZ_DIG; ++p)
+#pragma unroll
+            for (int kt = 0; kt < OZ_KC / 16; ++kt) {
+              // levels L = p..7 of A plane p against B planes 0..7-p; the
+              // first product of a window overwrites the accumulator
+              const uint32_t acc = (first && p == 0 && kt == 0) ? 0u : 1u;
+              asm volatile(
+                  "{\n .reg .pred pa;\n setp.ne.b32 pa, %4, 0;\n"
+                  " tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, pa;\n}" ::"r"(
+                      tmem + (uint32_t)(buf * OZ_ACC_COLS + p * OZ_N)),
+                  "l"(sdesc(a0 + p * OZ_A_TILE + kt * 256)), "l"(sdesc(b0 + kt * 256)),
+                  "r"(oz_idesc((OZ_LEVELS - p) * OZ_N)), "r"(acc));
+            }
+          mma_commit(BAR(OZ_B_EMPTY, s));
+          last_bar = BAR(OZ_B_EMPTY, s);
+          last_par = (uint32_t)(c >> 1) & 1u;
+          if (c % OZ_WINDOW == OZ_WINDOW - 1 || c == nchunks - 1) mma_commit(BAR(OZ_B_ACCF, buf));
+        } else {
+          atomicExch(sflag, 1);
+        }
+      }
+      if (!__shfl_sync(0xffffffffu, (int)ok, 0)) break;
+    }
+    // before the tensor memory is freed, every MMA issued must have completed
+    if (lane == 0 && last_bar != 0 && !mbar_drain(last_bar, last_par)) atomicExch(sflag, 1);
+    __syncwarp();
+  } else if (warp == OZ_LOAD_WARP) {
+    // ---- load warp: raw rows of chunk cc into raw stage cc % nraw ---------
+    // A block whose rows are contiguous (row stride = width) and 16-byte
+    // aligned comes in with one bulk copy; any other block is copied by the
+    // lanes.  Rows past r1 are not copied: the split reads them as zeros.
     const int nblk = *snblk;
-    // raw rows of chunk cc into raw stage rs.  A block whose rows are
-    // contiguous (row stride = width) and 16-byte aligned comes in with one
-    // bulk copy issued by thread 0 and completing on rawbar[rs]; any other
-    // block is copied by all splitters with plain loads and stores, visible
-    // after the next splitter barrier.  Rows past r1 are not copied: the
-    // split reads them as zeros.
-    auto load_chunk = [&](int cc, int rs) {
+    int issued = 0;
+    for (int cc = 0; cc < nchunks; ++cc) {
+      const int rs = cc % nraw;
+      const bool ok = cc < nraw || mbar_wait(BAR(OZ_B_RAWE, rs), (uint32_t)(cc / nraw - 1) & 1u, sflag);
+      if (!__all_sync(0xffffffffu, ok)) {
+        if (lane == 0) atomicExch(sflag, 1);
+        break;
+      }
       double* dst0 = raw + (size_t)rs * g.raw_stride;
       const int64_t rb = r0 + (int64_t)cc * OZ_KC;
       const int nrow = (int)min((int64_t)OZ_KC, r1 - rb);
-      if (tid == 0) {
-        uint32_t bytes = 0;
-        for (int k = 0; k < nblk; ++k) {
-          const uint32_t nb = (uint32_t)(nrow * bw[k] * 8);
-          const double* src = bsrc[k] + rb * bld[k];
-          if (bld[k] == bw[k] && ((uintptr_t)src & 15) == 0 && (nb & 15) == 0) bytes += nb;
+      uint32_t bytes = 0;
+      for (int k = 0; k < nblk; ++k) {
+        const uint32_t nb = (uint32_t)(nrow * bw[k] * 8);
+        const double* src = bsrc[k] + rb * bld[k];
+        if (bld[k] == bw[k] && ((uintptr_t)src & 15) == 0 && (nb & 15) == 0) {
+          bytes += nb;
+        } else {
+          for (int t = lane; t < nrow * bw[k]; t += 32) {
+            const int rr = t / bw[k], j = t - rr * bw[k];
+            dst0[boff[k] + t] = src[(int64_t)rr * bld[k] + j];
+          }
         }
+      }
+      __syncwarp();
+      if (lane == 0) {
         asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-        asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(rawb0 + 8 * rs), "r"(bytes)
+        asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(BAR(OZ_B_RAWF, rs)), "r"(bytes)
                      : "memory");
         for (int k = 0; k < nblk; ++k) {
           const uint32_t nb = (uint32_t)(nrow * bw[k] * 8);
@@ -311,141 +470,16 @@ __global__ void __launch_bounds__(OZ_THREADS, 1) k_gram_oz(OzArgs g) {
             asm volatile(
                 "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
                     smem_u32(dst0 + boff[k])),
-                "l"(src), "r"(nb), "r"(rawb0 + 8 * rs)
+                "l"(src), "r"(nb), "r"(BAR(OZ_B_RAWF, rs))
                 : "memory");
         }
       }
-      for (int k = 0; k < nblk; ++k) {
-        const uint32_t nb = (uint32_t)(nrow * bw[k] * 8);
-        const double* src = bsrc[k] + rb * bld[k];
-        if (bld[k] == bw[k] && ((uintptr_t)src & 15) == 0 && (nb & 15) == 0) continue;
-        for (int t = tid; t < nrow * bw[k]; t += OZ_SPLIT) {
-          const int rr = t / bw[k], j = t - rr * bw[k];
-          dst0[boff[k] + t] = src[(int64_t)rr * bld[k] + j];
-        }
-      }
-    };
-    const int ntask = 4 * rw;  // (column, group of 8 rows) per chunk
-    const int nraw = g.nraw;
-    for (int cc = 0; cc + 1 < nraw && cc < nchunks; ++cc) load_chunk(cc, cc);  // ring of nraw raw stages
-    for (int c = 0; c < nchunks; ++c) {
-      const int s = c & 1, rs = c % nraw;
-      const bool failed = *(volatile int*)sflag != 0;
-      // every splitter is done with the raw stage of chunk c - 1 (and the
-      // plain copies of chunk c, made one iteration ago, are visible); then
-      // the rows of chunk c + nraw - 1 are fetched into that stage
-      asm volatile("bar.sync 1, %0;" ::"r"(OZ_SPLIT) : "memory");
-      if (c + nraw - 1 < nchunks && *(volatile int*)sflag == 0) load_chunk(c + nraw - 1, (c + nraw - 1) % nraw);
-      if (nraw == 1) asm volatile("bar.sync 1, %0;" ::"r"(OZ_SPLIT) : "memory");  // plain copies of chunk c
-      // chunk c's bulk copies have landed
-      if (!failed && !mbar_wait(rawb0 + 8 * rs, (uint32_t)(c / nraw) & 1u)) atomicExch(sflag, 1);
-      // flush window w = c / 4 - 1 two chunks after it ended (warps 0-3), when
-      // its MMAs have long completed, so the split of chunk c is not held up
-      if (warp < 4 && c % OZ_WINDOW == 2 && c >= OZ_WINDOW + 2 && !failed) {
-        const int w = c / OZ_WINDOW - 1, buf = w & 1;
-        const bool ok = mbar_wait(accf0 + 8 * buf, (uint32_t)(w >> 1) & 1u);
-        if (!ok) atomicExch(sflag, 1);
-        asm volatile("tcgen05.fence::after_thread_sync;");
-        if (__all_sync(0xffffffffu, ok)) {
-#pragma unroll 1
-          for (int L = 0; L < OZ_LEVELS / 2; ++L) oz_flush_level(tmem, warp, buf, L, 7 * (3 - L), hi);
-#pragma unroll 1
-          for (int L = OZ_LEVELS / 2; L < OZ_LEVELS; ++L) oz_flush_level(tmem, warp, buf, L, 7 * (7 - L), lo);
-        }
-        asm volatile("tcgen05.fence::before_thread_sync;");
-        mbar_arrive(acce0 + 8 * buf);
-      }
-      // the MMAs of chunk c - 2 are done with digit stage s
-      if (c >= 2 && !failed && !mbar_wait(empty0 + 8 * s, (uint32_t)((c >> 1) - 1) & 1u)) atomicExch(sflag, 1);
-      if (*(volatile int*)sflag == 0) {
-        uint8_t* sa = tiles + s * OZ_STAGE;
-        uint8_t* sb = sa + OZ_DIG * OZ_A_TILE + (OZ_DIG - 1) * OZ_B_TILE;  // B plane 0
-        const double* rsrc = raw + (size_t)rs * g.raw_stride;
-        const int nrow = (int)min((int64_t)OZ_KC, r1 - (r0 + (int64_t)c * OZ_KC));
-        for (int t = tid; t < ntask; t += OZ_SPLIT) {
-          const int col = t % rw, g8 = t / rw;
-          const bool isA = col < m;
-          const int cc = isA ? col : col - m;
-          const int eb = isA ? sE[cc] : sE[OZ_M + cc];
-          const double* xs = rsrc + coff[col] + 8 * g8 * cw[col];
-          const int wcol = cw[col];
-          uint32_t pk[OZ_DIG][4];
-#pragma unroll
-          for (int k = 0; k < 8; k += 2) {
-            float d0[OZ_DIG], d1[OZ_DIG];
-            oz_digits(8 * g8 + k < nrow ? xs[k * wcol] : 0.0, eb, d0);
-            oz_digits(8 * g8 + k + 1 < nrow ? xs[(k + 1) * wcol] : 0.0, eb, d1);
-#pragma unroll
-            for (int p = 0; p < OZ_DIG; ++p) pk[p][k >> 1] = bf16x2(d0[p], d1[p]);
-          }
-          uint8_t* dst = isA ? sa : sb;
-          const int tile = isA ? OZ_A_TILE : OZ_B_TILE;
-          const int off = kmaj(cc, 8 * g8);  // 8 rows of one column: one 16-byte core row
-#pragma unroll
-          for (int p = 0; p < OZ_DIG; ++p)
-            *reinterpret_cast<uint4*>(dst + p * tile + off) = make_uint4(pk[p][0], pk[p][1], pk[p][2], pk[p][3]);
-        }
-      }
-      asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-      mbar_arrive(full0 + 8 * s);
+      issued = cc + 1;
     }
-    // the windows not flushed in the loop (the in-loop flushes covered
-    // windows 0 .. (nchunks - 3) / 4 - 1)
-    const int wdone = nchunks >= OZ_WINDOW + 3 ? (nchunks - 3) / OZ_WINDOW : 0;
-    for (int w = wdone; w < nwin && warp < 4; ++w) {
-      if (*(volatile int*)sflag != 0) break;
-      const int buf = w & 1;
-      const bool ok = mbar_wait(accf0 + 8 * buf, (uint32_t)(w >> 1) & 1u);
-      if (!ok) atomicExch(sflag, 1);
-      asm volatile("tcgen05.fence::after_thread_sync;");
-      if (__all_sync(0xffffffffu, ok)) {
-#pragma unroll 1
-        for (int L = 0; L < OZ_LEVELS / 2; ++L) oz_flush_level(tmem, warp, buf, L, 7 * (3 - L), hi);
-#pragma unroll 1
-        for (int L = OZ_LEVELS / 2; L < OZ_LEVELS; ++L) oz_flush_level(tmem, warp, buf, L, 7 * (7 - L), lo);
-      }
-      asm volatile("tcgen05.fence::before_thread_sync;");
-      mbar_arrive(acce0 + 8 * buf);
-    }
-  } else {
-    // ---- MMA warp: lane 0 issues, the warp stays converged ----------------
-    uint32_t last_bar = 0, last_par = 0;  // the latest commit: its completion covers every MMA
-    for (int c = 0; c < nchunks; ++c) {
-      const int s = c & 1, w = c / OZ_WINDOW, buf = w & 1;
-      bool ok = *(volatile int*)sflag == 0;
-      if (lane == 0 && ok) {
-        // accumulator buffer flushed (window w - 2), digit stage s full
-        if (c % OZ_WINDOW == 0 && w >= 2 && !mbar_wait(acce0 + 8 * buf, (uint32_t)((w >> 1) - 1) & 1u)) ok = false;
-        if (ok && !mbar_wait(full0 + 8 * s, (uint32_t)(c >> 1) & 1u)) ok = false;
-        if (!ok) atomicExch(sflag, 1);
-      }
-      if (lane == 0 && ok) {
-        asm volatile("tcgen05.fence::after_thread_sync;");
-        const bool first = (c % OZ_WINDOW) == 0;
-        const uint32_t a0 = smem_u32(tiles + s * OZ_STAGE);
-        const uint32_t bz = a0 + OZ_DIG * OZ_A_TILE;  // the zero tiles, then B planes 0..7
-#pragma unroll 1
-        for (int p = 0; p < OZ_DIG; ++p)
-#pragma unroll
-          for (int kt = 0; kt < OZ_KC / 16; ++kt) {
-            // levels L = 0..7 of A plane p against B planes L - p: the first
-            // product of a window overwrites the accumulator
-            const uint32_t acc = (first && p == 0 && kt == 0) ? 0u : 1u;
-            asm volatile(
-                "{\n .reg .pred pa;\n setp.ne.b32 pa, %4, 0;\n"
-                " tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, pa;\n}" ::"r"(tmem + (uint32_t)(buf * OZ_ACC_COLS)),
-                "l"(sdesc(a0 + p * OZ_A_TILE + kt * 256)), "l"(sdesc(bz + (OZ_DIG - 1 - p) * OZ_B_TILE + kt * 256)),
-                "r"(OZ_IDESC), "r"(acc));
-          }
-        mma_commit(empty0 + 8 * s);
-        last_bar = empty0 + 8 * s;
-        last_par = (uint32_t)(c >> 1) & 1u;
-        if (c % OZ_WINDOW == OZ_WINDOW - 1 || c == nchunks - 1) mma_commit(accf0 + 8 * buf);
-      }
-      __syncwarp();
-    }
-    // before the tensor memory is freed, every MMA issued must have completed
-    if (lane == 0 && last_bar != 0 && !mbar_wait(last_bar, last_par)) atomicExch(sflag, 1);
+    // the copies still in flight land before the CTA may exit
+    if (lane == 0)
+      for (int cc = max(0, issued - nraw); cc < issued; ++cc)
+        if (!mbar_drain(BAR(OZ_B_RAWF, cc % nraw), (uint32_t)(cc / nraw) & 1u)) atomicExch(sflag, 1);
     __syncwarp();
   }
   asm volatile("tcgen05.fence::before_thread_sync;");
@@ -453,8 +487,8 @@ __global__ void __launch_bounds__(OZ_THREADS, 1) k_gram_oz(OzArgs g) {
   asm volatile("tcgen05.fence::after_thread_sync;");
   const bool ok = *(volatile int*)sflag == 0;
   if (!ok && tid == 0) atomicExch(g.status, 1);
-  if (warp < 4) {
-    const int i = warp * 32 + lane;
+  if (warp >= OZ_FLUSH_WARP && warp < OZ_MMA_WARP) {
+    const int i = (warp & 3) * 32 + lane;
     if (i < m)
 #pragma unroll
       for (int j = 0; j < OZ_N; ++j)
@@ -464,34 +498,38 @@ __global__ void __launch_bounds__(OZ_THREADS, 1) k_gram_oz(OzArgs g) {
           g.partial[((int64_t)blockIdx.x * m + i) * nbc + j] = ok ? v : 0.0;
         }
   }
-  if (warp == 8) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(OZ_TMEM_COLS));
+  if (warp == OZ_MMA_WARP)
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(OZ_TMEM_COLS));
 }
 
-// biased max exponent of each column (nsd columns per block, rows ld values
-// apart, nblk blocks sX apart) into E[col0 + block * nsd + s] (atomicMax; E
-// must be zeroed first).  Order-independent, hence deterministic.
-__global__ void k_col_maxexp(const double* X, int nblk, int64_t sX, int nsd, int ld, int64_t N, int* E, int col0,
-                             const int* skip) {
+// biased max exponent of each column (nsd <= 256 columns per block, rows ld
+// values apart, nblk blocks sX apart) into E[col0 + block * nsd + s]
+// (atomicMax; E must be zeroed first).  Thread t of a CTA keeps column
+// t % nsd of the CTA's rows t / nsd, + rows per pass, ...: consecutive
+// threads read consecutive values of a row.  Order-independent, hence
+// deterministic.
+__global__ void __launch_bounds__(256) k_col_maxexp(const double* X, int nblk, int64_t sX, int nsd, int ld, int64_t N,
+                                                    int* E, int col0, const int* skip) {
   if (skip && *skip) return;
+  __shared__ int smax[256];
+  const int rpp = blockDim.x / nsd;  // rows per pass of one CTA
+  const int c = threadIdx.x % nsd, rl = threadIdx.x / nsd;
+  const int64_t rstep = (int64_t)gridDim.x * rpp;
   for (int b = 0; b < nblk; ++b) {
     const double* x = X + (int64_t)b * sX;
-    for (int s0 = 0; s0 < nsd; s0 += 8) {
-      int mx[8] = {0, 0, 0, 0, 0, 0, 0, 0};
-      for (int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; r < N; r += (int64_t)gridDim.x * blockDim.x)
-#pragma unroll
-        for (int s = 0; s < 8; ++s)
-          if (s0 + s < nsd) {
-            const int e = (int)(((unsigned long long)__double_as_longlong(x[r * ld + s0 + s]) >> 52) & 0x7FF);
-            mx[s] = max(mx[s], e);
-          }
-#pragma unroll
-      for (int s = 0; s < 8; ++s) {
-        int v = mx[s];
-#pragma unroll
-        for (int o = 16; o > 0; o >>= 1) v = max(v, __shfl_xor_sync(0xffffffffu, v, o));
-        if ((threadIdx.x & 31) == 0 && v > 0 && s0 + s < nsd) atomicMax(&E[col0 + b * nsd + s0 + s], v);
-      }
+    for (int i = threadIdx.x; i < nsd; i += blockDim.x) smax[i] = 0;
+    __syncthreads();
+    int mx = 0;
+    if (rl < rpp) {
+#pragma unroll 4
+      for (int64_t r = (int64_t)blockIdx.x * rpp + rl; r < N; r += rstep)
+        mx = max(mx, (int)(((unsigned long long)__double_as_longlong(x[r * ld + c]) >> 52) & 0x7FF));
+      if (mx > 0) atomicMax(&smax[c], mx);
     }
+    __syncthreads();
+    for (int i = threadIdx.x; i < nsd; i += blockDim.x)
+      if (smax[i] > 0) atomicMax(&E[col0 + b * nsd + i], smax[i]);
+    __syncthreads();
   }
 }
 
@@ -525,7 +563,7 @@ int qp_gram_oz_prepare() {
 
 void qp_col_maxexp(const double* X, int nblk, int64_t sX, int nsd, int ld, int64_t N, int* E, int col0,
                    const int* skip, cudaStream_t st, int n_sm) {
-  k_col_maxexp<<<2 * n_sm, 256, 0, st>>>(X, nblk, sX, nsd, ld, N, E, col0, skip);
+  k_col_maxexp<<<4 * n_sm, 256, 0, st>>>(X, nblk, sX, nsd, ld, N, E, col0, skip);
 }
 
 // X (m x nbc, row-major) = A^T [B0 B1] per CTA into partial[cta][m][nbc];
@@ -557,9 +595,22 @@ void qp_gram_oz(const double* A, int64_t sA, int m, int nsdA, int ldA, const dou
   g.status = status;
   // raw stages of OZ_KC rows of the m + nbc columns (256-byte aligned): as
   // many as fit beside the digit stages, up to OZ_MAXRAW
-  g.raw_stride = (OZ_KC * (m + nbc) + 31) / 32 * 32;
+  const int rw = m + nbc;
+  g.raw_stride = (OZ_KC * rw + 31) / 32 * 32;
   g.nraw = std::max(1, std::min(OZ_MAXRAW, (OZ_SMEM_MAX - 2 * OZ_STAGE - OZ_TAB) / (g.raw_stride * 8)));
   const int smem = 2 * OZ_STAGE + g.nraw * g.raw_stride * 8 + OZ_TAB;
+  // rows per splitting task: the fewest rows per thread on the longest
+  // thread's path (more, narrower stores only where that gains)
+  int best = 1 << 30;
+  g.rpt = 8;
+  for (int r : {8, 4, 2}) {
+    const int ntask = rw * (OZ_KC / r);
+    const int cost = (ntask + OZ_SPLIT - 1) / OZ_SPLIT * r * 4 + (8 / r);
+    if (cost < best) {
+      best = cost;
+      g.rpt = r;
+    }
+  }
   k_gram_oz<<<ncta, OZ_THREADS, smem, st>>>(g);
 }
 
