@@ -331,6 +331,28 @@ int qpgpu_connected_pairs(qpgpu_ctx* ctx, int64_t* n_pairs, int32_t* I, int32_t*
 int qpgpu_connected_pairs_rows(qpgpu_ctx* ctx, const int32_t* rows, int64_t n_rows, int64_t* n_pairs, int32_t* I,
                                int32_t* J, int8_t* cls, int8_t* phase, int16_t* exc, double* hij, int64_t cap);
 
+/* CIPSI selection with the Epstein-Nesbet second-order energy over the
+ * context's wave function, which must be in psi_det_sorted order: the
+ * generators are determinants 0..n_gen-1 and the selectors 0..n_sel-1
+ * (1 <= n_gen <= n_sel <= N_det).  Replaces select_connected and the walk it
+ * drives (plugins/Full_CI_ZMQ/selection.irp.f:24-79, :258-1172).  Holes are
+ * every occupied orbital of a generator and particles every empty one (the
+ * full generators_bitmask of Full_CI).  coef (N_det, n_st) is column-major
+ * (psi_coef_sorted) and e0 (n_st) holds the denominators (pt2_E0_denominator,
+ * electronic).  Every determinant a outside the wave function within a double
+ * excitation of a generator is counted once, by the first generator that
+ * reaches it, with the numerators mat(st) = sum over the selectors of
+ * c_D,st <a|H|D>.  Each such a with a non-zero numerator adds
+ * e = (sign(d) sqrt(d^2 + 4 mat^2) - d) / 2 (d = e0 - H_aa,
+ * fill_buffer_double, :582-645) to pt2 (n_st).  The buffer keeps the
+ * buf_size most negative values min(0, min_st e) (selection_buffer.irp.f),
+ * ascending, ties in determinant-bit order, with their determinants
+ * (N_int, 2) each in buf_dets.  *n_ext returns the number of external
+ * determinants with a non-zero numerator.  1 <= n_st <= 8.  Returns the
+ * number of buffer entries written (>= 0) or a negative status. */
+int qpgpu_select_pt2(qpgpu_ctx* ctx, const double* coef, int n_st, const double* e0, int n_gen, int n_sel,
+                     int buf_size, double* pt2, uint64_t* buf_dets, double* buf_vals, int64_t* n_ext);
+
 #ifdef __cplusplus
 }
 #endif

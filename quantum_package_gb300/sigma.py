@@ -165,6 +165,29 @@ class Wavefunction:
         o = np.lexsort((J, I))
         return dict(I=I[o], J=J[o], cls=cls[o], phase=ph[o], exc=exc[o], hij=hij[o])
 
+    # --- CIPSI selection ------------------------------------------------
+    def select_pt2(self, coef, e0, n_gen, n_sel, buf_size):
+        """Selection with the second-order energy (qpgpu_select_pt2) over this
+        set, which must be in psi_det_sorted order.  coef: (n_st, N) (the
+        sorted coefficients), e0: (n_st,) electronic denominators.  Returns
+        (pt2 (n_st,), buffer determinants (k, 2, N_int), buffer values (k,),
+        number of external determinants with a non-zero numerator)."""
+        cm = np.ascontiguousarray(np.atleast_2d(coef), dtype=np.float64)
+        n_st = cm.shape[0]
+        e0 = np.ascontiguousarray(np.atleast_1d(e0), dtype=np.float64)
+        if e0.shape != (n_st,) or cm.shape[1] != self.n_det:
+            raise ValueError("select_pt2: coef must be (n_st, N_det) and e0 (n_st,)")
+        nint = self.n_int
+        pt2 = np.zeros(n_st)
+        bd = np.zeros((max(buf_size, 1), 2, nint), np.uint64)
+        bv = np.zeros(max(buf_size, 1))
+        n_ext = C.c_int64()
+        rc = _lib.load().qpgpu_select_pt2(self._ctx, _p(cm), n_st, _p(e0), int(n_gen), int(n_sel), int(buf_size),
+                                          _p(pt2), _p(bd), _p(bv), C.byref(n_ext))
+        if rc < 0:
+            check(rc, self._ctx)
+        return pt2, bd[:rc].copy(), bv[:rc].copy(), n_ext.value
+
     # --- dressing (MRCC / MRCEPA0) ---------------------------------------
     def set_dressing(self, idx_ref, idx_non_ref, delta_ij, delta_ij_s2, delta_ii=None):
         """Dressing of one state (delta_ij(istate,:,:) of the reference's providers):
