@@ -353,6 +353,17 @@ int qpgpu_connected_pairs_rows(qpgpu_ctx* ctx, const int32_t* rows, int64_t n_ro
 int qpgpu_select_pt2(qpgpu_ctx* ctx, const double* coef, int n_st, const double* e0, int n_gen, int n_sel,
                      int buf_size, double* pt2, uint64_t* buf_dets, double* buf_vals, int64_t* n_ext);
 
+/* The second-order energy of each listed generator separately (pt2_detail of
+ * the stochastic PT2, plugins/Full_CI_ZMQ/pt2_stoch_routines.irp.f:6-155,
+ * which runs select_connected on sampled generators).  gens[0..n_list) are
+ * 0-based psi_det indices below n_sel.  Generator g gets the contributions
+ * of the external determinants it reaches first: the same rules and
+ * arguments as qpgpu_select_pt2, with every generator before g banning,
+ * listed or not.  pt2_detail is (n_list, n_st) row-major (state fastest).
+ * The comb sampling that picks the generators is host logic. */
+int qpgpu_pt2_generators(qpgpu_ctx* ctx, const double* coef, int n_st, const double* e0, int n_sel,
+                         const int32_t* gens, int n_list, double* pt2_detail);
+
 #ifdef __cplusplus
 }
 #endif

@@ -66,7 +66,8 @@ constexpr int SEL_MAXFG = 2048;    // earlier generators kept per item (checked,
 enum { IT_SINGLE = 0, IT_SAME = 1, IT_AB = 2 };
 
 struct SelItem {
-  int g;
+  int g;         // generator (psi_det index)
+  int gl;        // its position in the generator list of the call
   int kind;      // IT_*
   int spin;      // single / same-spin double: 0 alpha, 1 beta
   int h1, h2;    // holes (1-based); alpha-beta: h1 alpha, h2 beta
@@ -81,11 +82,11 @@ struct SelArgs {
   int n_st;
   int64_t N;
   const SelItem* items;
-  const int64_t* ilist_off;  // per generator: selectors within a quadruple excitation
+  const int64_t* ilist_off;  // per listed generator: selectors within a quadruple excitation
   const int* ilist;
-  const int64_t* flist_off;  // per generator: earlier generators within a quadruple excitation
+  const int64_t* flist_off;  // per listed generator: earlier generators within a quadruple excitation
   const int* flist;
-  const double* fock;        // per generator: build_fock_tmp, [g][2][n_mo + 2]
+  const double* fock;        // per listed generator: build_fock_tmp, [gl][2][n_mo + 2]
   const int* hslot;          // hash set of psi_det: det index or -1
   uint64_t hmask;
   double* pt2_part;          // [item][n_st]
@@ -149,16 +150,18 @@ __device__ __forceinline__ int exc_deg(const u64* a, const u64* b) {
   return d >> 1;
 }
 
-// per generator g: the candidates c < limit (selectors: limit = n_sel;
-// earlier generators: limit = g) within a quadruple excitation of g, in
-// increasing order.  mode 0 counts, mode 1 fills at off[g].
+// per listed generator g = gens[l]: the candidates c < limit (selectors:
+// limit = n_sel; earlier generators: limit = g) within a quadruple excitation
+// of g, in increasing order.  mode 0 counts into cnt[l], mode 1 fills at off[l].
 template <int NINT>
-__global__ void __launch_bounds__(SBLK) k_sel_lists(const u64* dets, int n_gen, int n_sel, int earlier, int mode,
-                                                    int64_t* cnt, const int64_t* off, int* out) {
+__global__ void __launch_bounds__(SBLK) k_sel_lists(const u64* dets, const int* gens, int n_list, int n_sel,
+                                                    int earlier, int mode, int64_t* cnt, const int64_t* off,
+                                                    int* out) {
   __shared__ int wsum[SBLK / 32];
   __shared__ int base_s;
-  const int g = blockIdx.x;
-  if (g >= n_gen) return;
+  const int l = blockIdx.x;
+  if (l >= n_list) return;
+  const int g = gens[l];
   u64 gd[2 * NINT];
 #pragma unroll
   for (int w = 0; w < 2 * NINT; ++w) gd[w] = dets[(int64_t)g * 2 * NINT + w];
@@ -175,7 +178,7 @@ __global__ void __launch_bounds__(SBLK) k_sel_lists(const u64* dets, int n_gen, 
     __syncthreads();
     int before = base_s;
     for (int w = 0; w < warp; ++w) before += wsum[w];
-    if (mode == 1 && keep) out[off[g] + before + __popc(bal & ((1u << lane) - 1))] = c;
+    if (mode == 1 && keep) out[off[l] + before + __popc(bal & ((1u << lane) - 1))] = c;
     __syncthreads();
     if (threadIdx.x == 0) {
       int tot = 0;
@@ -184,18 +187,18 @@ __global__ void __launch_bounds__(SBLK) k_sel_lists(const u64* dets, int n_gen, 
     }
     __syncthreads();
   }
-  if (mode == 0 && threadIdx.x == 0) cnt[g] = base_s;
+  if (mode == 0 && threadIdx.x == 0) cnt[l] = base_s;
 }
 
-// build_fock_tmp (Fock_diag.irp.f:1-98) of every generator:
-// f[g][s][i], i = 1..n_mo, and f[g][s][n_mo + 1] = <g|H|g>
+// build_fock_tmp (Fock_diag.irp.f:1-98) of every listed generator:
+// f[l][s][i], i = 1..n_mo, and f[l][s][n_mo + 1] = <g|H|g>
 template <int NINT>
-__global__ void k_sel_fock(DevTables t, const u64* dets, int n_gen, double* fock) {
-  const int g = blockIdx.x * blockDim.x + threadIdx.x;
-  if (g >= n_gen) return;
+__global__ void k_sel_fock(DevTables t, const u64* dets, const int* gens, int n_list, double* fock) {
+  const int l = blockIdx.x * blockDim.x + threadIdx.x;
+  if (l >= n_list) return;
   const int n = t.n, st = n + 2;
-  const u64* d = dets + (int64_t)g * 2 * NINT;
-  double* f = fock + (int64_t)g * 2 * st;
+  const u64* d = dets + (int64_t)gens[l] * 2 * NINT;
+  double* f = fock + (int64_t)l * 2 * st;
   for (int i = 0; i < 2 * st; ++i) f[i] = 0.0;
   int occ[2][QPGPU_MAX_MO];
   int no[2] = {0, 0};
@@ -312,7 +315,7 @@ __global__ void __launch_bounds__(SBLK) k_sel_items(SelArgs A) {
   __syncthreads();
   // the earlier generators that can reach a determinant of this item
   {
-    const int64_t f0 = A.flist_off[it.g], f1 = A.flist_off[it.g + 1];
+    const int64_t f0 = A.flist_off[it.gl], f1 = A.flist_off[it.gl + 1];
     for (int64_t f = f0 + tid; f < f1; f += SBLK) {
       const int gp = A.flist[f];
       const u64* q = A.dets + (int64_t)gp * 2 * NINT;
@@ -349,7 +352,7 @@ __global__ void __launch_bounds__(SBLK) k_sel_items(SelArgs A) {
       p2 = vir[1][e % nb];
     }
   };
-  const int64_t i0 = A.ilist_off[it.g], i1 = A.ilist_off[it.g + 1];
+  const int64_t i0 = A.ilist_off[it.gl], i1 = A.ilist_off[it.gl + 1];
   for (int64_t base = i0; base < i1; base += SEL_DTILE) {
     // stage the selectors of this pass with k = |mask \ D| <= 2, in order
     if (tid == 0) nsel_s = 0;
@@ -417,7 +420,7 @@ __global__ void __launch_bounds__(SBLK) k_sel_items(SelArgs A) {
 #pragma unroll
   for (int s = 0; s < SEL_MAXST; ++s) pt[s] = 0.0;
   const int st = n + 2;
-  const double* F = A.fock + (int64_t)it.g * 2 * st;
+  const double* F = A.fock + (int64_t)it.gl * 2 * st;
   const double eg = F[n + 1];
   unsigned long long next = 0;
   for (int e = tid; e < ne; e += SBLK) {
@@ -519,25 +522,27 @@ struct Dev {
 
 }  // namespace
 
-extern "C" int qpgpu_select_pt2(qpgpu_ctx* c, const double* coef, int n_st, const double* e0, int n_gen, int n_sel,
-                                int buf_size, double* pt2, uint64_t* buf_dets, double* buf_vals, int64_t* n_ext) {
-  if (!c) return QPGPU_ERR_ARG;
-  if (!coef || !e0 || !pt2 || n_st < 1 || n_st > SEL_MAXST || buf_size < 0 ||
-      (buf_size > 0 && (!buf_dets || !buf_vals)))
-    return qpgpu_fail(c, QPGPU_ERR_ARG, "select_pt2: bad arguments (1 <= n_st <= 8, buffers for buf_size > 0)");
-  std::lock_guard<std::mutex> lk(c->mu);
-  if (!c->have_ints || !c->have_dets) return qpgpu_fail(c, QPGPU_ERR_STATE, "select_pt2: integrals and determinants first");
+// The selection over the listed generators (psi_det indices, each banned by
+// every generator before it, listed or not).  pt2 (n_st) sums all of them;
+// per_gen (n_list x n_st, optional) holds each generator's share, summed over
+// its items in order.  The buffer as qpgpu_select_pt2.  Returns the number of
+// buffer entries written or a negative status.
+static int run_selection(qpgpu_ctx* c, const double* coef, int n_st, const double* e0, int n_sel,
+                         const std::vector<int>& gens, int buf_size, double* pt2, double* per_gen,
+                         uint64_t* buf_dets, double* buf_vals, int64_t* n_ext) {
   const int64_t N = c->N;
-  if (n_gen < 1 || n_gen > n_sel || n_sel > N)
-    return qpgpu_fail(c, QPGPU_ERR_ARG, "select_pt2: need 1 <= n_gen <= n_sel <= N_det");
   const int nint = c->nint, n = c->n_mo;
+  const int n_list = (int)gens.size();
   cudaStream_t st = c->stream;
-  // host copies of the generators (item list, virtual counts)
-  std::vector<u64> gdet((size_t)n_gen * 2 * nint);
-  QP_CUDA(c, cudaMemcpyAsync(gdet.data(), c->d_dets, gdet.size() * sizeof(u64), cudaMemcpyDeviceToHost, st));
+  // host copies of the listed generators (item list)
+  std::vector<u64> gdet((size_t)n_list * 2 * nint);
+  for (int l = 0; l < n_list; ++l)
+    QP_CUDA(c, cudaMemcpyAsync(&gdet[(size_t)l * 2 * nint], c->d_dets + (int64_t)gens[l] * 2 * nint,
+                               2 * nint * sizeof(u64), cudaMemcpyDeviceToHost, st));
   QP_CUDA(c, cudaStreamSynchronize(st));
   const int tile_entries = SEL_TILE / n_st;
   std::vector<SelItem> items;
+  std::vector<int64_t> item_first(n_list + 1);
   auto push = [&](SelItem it, int ne) {
     for (int a = 0; a < ne; a += tile_entries) {
       it.e0 = a;
@@ -545,29 +550,41 @@ extern "C" int qpgpu_select_pt2(qpgpu_ctx* c, const double* coef, int n_st, cons
       items.push_back(it);
     }
   };
-  for (int g = 0; g < n_gen; ++g) {
+  for (int l = 0; l < n_list; ++l) {
+    item_first[l] = (int64_t)items.size();
+    const int g = gens[l];
     std::vector<int> occ[2];
     for (int s = 0; s < 2; ++s)
       for (int o = 1; o <= n; ++o)
-        if ((gdet[(size_t)g * 2 * nint + s * nint + ((o - 1) >> 6)] >> ((o - 1) & 63)) & 1ull) occ[s].push_back(o);
+        if ((gdet[(size_t)l * 2 * nint + s * nint + ((o - 1) >> 6)] >> ((o - 1) & 63)) & 1ull) occ[s].push_back(o);
     const int nv[2] = {n - (int)occ[0].size(), n - (int)occ[1].size()};
     for (int s = 0; s < 2; ++s)
-      for (int h : occ[s]) push(SelItem{g, IT_SINGLE, s, h, 0, 0, 0}, nv[s]);
+      for (int h : occ[s]) push(SelItem{g, l, IT_SINGLE, s, h, 0, 0, 0}, nv[s]);
     for (int s = 0; s < 2; ++s)
       for (size_t x = 0; x < occ[s].size(); ++x)
         for (size_t y = x + 1; y < occ[s].size(); ++y)
-          push(SelItem{g, IT_SAME, s, occ[s][x], occ[s][y], 0, 0}, nv[s] * (nv[s] - 1) / 2);
+          push(SelItem{g, l, IT_SAME, s, occ[s][x], occ[s][y], 0, 0}, nv[s] * (nv[s] - 1) / 2);
     for (int ha : occ[0])
-      for (int hb : occ[1]) push(SelItem{g, IT_AB, 0, ha, hb, 0, 0}, nv[0] * nv[1]);
+      for (int hb : occ[1]) push(SelItem{g, l, IT_AB, 0, ha, hb, 0, 0}, nv[0] * nv[1]);
   }
+  item_first[n_list] = (int64_t)items.size();
   const int64_t n_items = (int64_t)items.size();
+  for (int s = 0; s < n_st; ++s) pt2[s] = 0.0;
+  if (n_ext) *n_ext = 0;
+  if (n_items == 0) {
+    if (per_gen)
+      for (size_t x = 0; x < (size_t)n_list * n_st; ++x) per_gen[x] = 0.0;
+    return 0;
+  }
   // device arrays
-  Dev d_items, d_coef, d_e0, d_icnt, d_ioff, d_ilist, d_fcnt, d_foff, d_flist, d_fock, d_slot, d_part, d_cnt, d_err,
-      d_pt2;
+  Dev d_items, d_gens, d_coef, d_e0, d_icnt, d_ioff, d_ilist, d_fcnt, d_foff, d_flist, d_fock, d_slot, d_part, d_cnt,
+      d_err, d_pt2;
   uint64_t hcap = 1;
   while (hcap < (uint64_t)(2 * N)) hcap <<= 1;
   QP_CUDA(c, cudaMalloc(&d_items.p, items.size() * sizeof(SelItem)));
   QP_CUDA(c, cudaMemcpyAsync(d_items.p, items.data(), items.size() * sizeof(SelItem), cudaMemcpyHostToDevice, st));
+  QP_CUDA(c, cudaMalloc(&d_gens.p, n_list * sizeof(int)));
+  QP_CUDA(c, cudaMemcpyAsync(d_gens.p, gens.data(), n_list * sizeof(int), cudaMemcpyHostToDevice, st));
   // coefficients: column-major (N, n_st) on the host -> (N, n_st) row-major
   std::vector<double> crow((size_t)N * n_st);
   for (int s = 0; s < n_st; ++s)
@@ -578,22 +595,22 @@ extern "C" int qpgpu_select_pt2(qpgpu_ctx* c, const double* coef, int n_st, cons
   QP_CUDA(c, cudaMemcpyAsync(d_e0.p, e0, n_st * sizeof(double), cudaMemcpyHostToDevice, st));
   QP_CUDA(c, cudaMalloc(&d_slot.p, hcap * sizeof(int)));
   QP_CUDA(c, cudaMemsetAsync(d_slot.p, 0xff, hcap * sizeof(int), st));
-  QP_CUDA(c, cudaMalloc(&d_fock.p, (size_t)n_gen * 2 * (n + 2) * sizeof(double)));
-  QP_CUDA(c, cudaMalloc(&d_icnt.p, (n_gen + 1) * sizeof(int64_t)));
-  QP_CUDA(c, cudaMalloc(&d_fcnt.p, (n_gen + 1) * sizeof(int64_t)));
+  QP_CUDA(c, cudaMalloc(&d_fock.p, (size_t)n_list * 2 * (n + 2) * sizeof(double)));
+  QP_CUDA(c, cudaMalloc(&d_icnt.p, (n_list + 1) * sizeof(int64_t)));
+  QP_CUDA(c, cudaMalloc(&d_fcnt.p, (n_list + 1) * sizeof(int64_t)));
   QP_CUDA(c, cudaMalloc(&d_cnt.p, 2 * sizeof(unsigned long long)));
-  QP_CUDA(c, cudaMemsetAsync(d_cnt.p, 0, 2 * sizeof(unsigned long long), st));
   QP_CUDA(c, cudaMalloc(&d_err.p, sizeof(int)));
   QP_CUDA(c, cudaMemsetAsync(d_err.p, 0, sizeof(int), st));
   QP_CUDA(c, cudaMalloc(&d_pt2.p, n_st * sizeof(double)));
   QP_CUDA(c, cudaMalloc(&d_part.p, (size_t)n_items * n_st * sizeof(double)));
   const u64* dets = c->d_dets;
-  const int hb = std::min<int64_t>((N + 255) / 256, (int64_t)c->n_sm * 8);
+  const int* dg = (const int*)d_gens.p;
+  const int hb = (int)std::min<int64_t>((N + 255) / 256, (int64_t)c->n_sm * 8);
 #define QP_SEL_NINT(NI)                                                                                          \
   k_hash_insert<NI><<<hb, 256, 0, st>>>(dets, N, (int*)d_slot.p, hcap - 1);                                     \
-  k_sel_lists<NI><<<n_gen, SBLK, 0, st>>>(dets, n_gen, n_sel, 0, 0, (int64_t*)d_icnt.p, nullptr, nullptr);        \
-  k_sel_lists<NI><<<n_gen, SBLK, 0, st>>>(dets, n_gen, n_sel, 1, 0, (int64_t*)d_fcnt.p, nullptr, nullptr);        \
-  k_sel_fock<NI><<<(n_gen + 63) / 64, 64, 0, st>>>(c->tab, dets, n_gen, (double*)d_fock.p);
+  k_sel_lists<NI><<<n_list, SBLK, 0, st>>>(dets, dg, n_list, n_sel, 0, 0, (int64_t*)d_icnt.p, nullptr, nullptr); \
+  k_sel_lists<NI><<<n_list, SBLK, 0, st>>>(dets, dg, n_list, n_sel, 1, 0, (int64_t*)d_fcnt.p, nullptr, nullptr); \
+  k_sel_fock<NI><<<(n_list + 63) / 64, 64, 0, st>>>(c->tab, dets, dg, n_list, (double*)d_fock.p);
   if (nint == 1) {
     QP_SEL_NINT(1)
   } else {
@@ -601,26 +618,26 @@ extern "C" int qpgpu_select_pt2(qpgpu_ctx* c, const double* coef, int n_st, cons
   }
 #undef QP_SEL_NINT
   QP_CUDA(c, cudaGetLastError());
-  // list offsets on the host (n_gen values)
-  std::vector<int64_t> icnt(n_gen), fcnt(n_gen), ioff(n_gen + 1), foff(n_gen + 1);
-  QP_CUDA(c, cudaMemcpyAsync(icnt.data(), d_icnt.p, n_gen * sizeof(int64_t), cudaMemcpyDeviceToHost, st));
-  QP_CUDA(c, cudaMemcpyAsync(fcnt.data(), d_fcnt.p, n_gen * sizeof(int64_t), cudaMemcpyDeviceToHost, st));
+  // list offsets on the host
+  std::vector<int64_t> icnt(n_list), fcnt(n_list), ioff(n_list + 1), foff(n_list + 1);
+  QP_CUDA(c, cudaMemcpyAsync(icnt.data(), d_icnt.p, n_list * sizeof(int64_t), cudaMemcpyDeviceToHost, st));
+  QP_CUDA(c, cudaMemcpyAsync(fcnt.data(), d_fcnt.p, n_list * sizeof(int64_t), cudaMemcpyDeviceToHost, st));
   QP_CUDA(c, cudaStreamSynchronize(st));
   ioff[0] = foff[0] = 0;
-  for (int g = 0; g < n_gen; ++g) {
-    ioff[g + 1] = ioff[g] + icnt[g];
-    foff[g + 1] = foff[g] + fcnt[g];
+  for (int l = 0; l < n_list; ++l) {
+    ioff[l + 1] = ioff[l] + icnt[l];
+    foff[l + 1] = foff[l] + fcnt[l];
   }
-  QP_CUDA(c, cudaMalloc(&d_ioff.p, (n_gen + 1) * sizeof(int64_t)));
-  QP_CUDA(c, cudaMalloc(&d_foff.p, (n_gen + 1) * sizeof(int64_t)));
-  QP_CUDA(c, cudaMemcpyAsync(d_ioff.p, ioff.data(), (n_gen + 1) * sizeof(int64_t), cudaMemcpyHostToDevice, st));
-  QP_CUDA(c, cudaMemcpyAsync(d_foff.p, foff.data(), (n_gen + 1) * sizeof(int64_t), cudaMemcpyHostToDevice, st));
-  QP_CUDA(c, cudaMalloc(&d_ilist.p, std::max<int64_t>(1, ioff[n_gen]) * sizeof(int)));
-  QP_CUDA(c, cudaMalloc(&d_flist.p, std::max<int64_t>(1, foff[n_gen]) * sizeof(int)));
-  // candidates: at most one per entry
+  QP_CUDA(c, cudaMalloc(&d_ioff.p, (n_list + 1) * sizeof(int64_t)));
+  QP_CUDA(c, cudaMalloc(&d_foff.p, (n_list + 1) * sizeof(int64_t)));
+  QP_CUDA(c, cudaMemcpyAsync(d_ioff.p, ioff.data(), (n_list + 1) * sizeof(int64_t), cudaMemcpyHostToDevice, st));
+  QP_CUDA(c, cudaMemcpyAsync(d_foff.p, foff.data(), (n_list + 1) * sizeof(int64_t), cudaMemcpyHostToDevice, st));
+  QP_CUDA(c, cudaMalloc(&d_ilist.p, std::max<int64_t>(1, ioff[n_list]) * sizeof(int)));
+  QP_CUDA(c, cudaMalloc(&d_flist.p, std::max<int64_t>(1, foff[n_list]) * sizeof(int)));
+  // candidates (only when a buffer is asked for): at most one per entry
   uint64_t ub = 0;
   for (const SelItem& it : items) ub += (uint64_t)(it.e1 - it.e0);
-  uint64_t cap = std::min<uint64_t>(ub, 1ull << 24);
+  uint64_t cap = buf_size > 0 ? std::min<uint64_t>(ub, 1ull << 28) : 0;  // <= 10.7 GB of candidates
   Dev d_cval, d_cdet;
   SelArgs A{};
   A.t = c->tab;
@@ -654,10 +671,10 @@ extern "C" int qpgpu_select_pt2(qpgpu_ctx* c, const double* coef, int n_st, cons
     A.cand_det = (u64*)d_cdet.p;
     QP_CUDA(c, cudaMemsetAsync(d_cnt.p, 0, 2 * sizeof(unsigned long long), st));
 #define QP_SEL_RUN(NI)                                                                                             \
-  k_sel_lists<NI><<<n_gen, SBLK, 0, st>>>(dets, n_gen, n_sel, 0, 1, nullptr, (const int64_t*)d_ioff.p,             \
-                                          (int*)d_ilist.p);                                                        \
-  k_sel_lists<NI><<<n_gen, SBLK, 0, st>>>(dets, n_gen, n_sel, 1, 1, nullptr, (const int64_t*)d_foff.p,             \
-                                          (int*)d_flist.p);                                                        \
+  k_sel_lists<NI><<<n_list, SBLK, 0, st>>>(dets, dg, n_list, n_sel, 0, 1, nullptr, (const int64_t*)d_ioff.p,       \
+                                           (int*)d_ilist.p);                                                       \
+  k_sel_lists<NI><<<n_list, SBLK, 0, st>>>(dets, dg, n_list, n_sel, 1, 1, nullptr, (const int64_t*)d_foff.p,       \
+                                           (int*)d_flist.p);                                                       \
   QP_CUDA(c, cudaFuncSetAttribute(k_sel_items<NI>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));       \
   k_sel_items<NI><<<(unsigned)n_items, SBLK, smem, st>>>(A);
     if (nint == 1) {
@@ -669,7 +686,7 @@ extern "C" int qpgpu_select_pt2(qpgpu_ctx* c, const double* coef, int n_st, cons
     QP_CUDA(c, cudaGetLastError());
     QP_CUDA(c, cudaMemcpyAsync(hcnt, d_cnt.p, 2 * sizeof(unsigned long long), cudaMemcpyDeviceToHost, st));
     QP_CUDA(c, cudaStreamSynchronize(st));
-    if (hcnt[1] <= cap) break;
+    if (buf_size == 0 || hcnt[1] <= cap) break;
     cap = hcnt[1];  // every candidate counted: run once more with room for all of them
   }
   int herr = 0;
@@ -677,8 +694,19 @@ extern "C" int qpgpu_select_pt2(qpgpu_ctx* c, const double* coef, int n_st, cons
   if (herr) return qpgpu_fail(c, QPGPU_ERR_ARG, "select_pt2: more than 2048 earlier generators reach one work item");
   k_sel_pt2<<<1, 32, 0, st>>>((const double*)d_part.p, n_items, n_st, (double*)d_pt2.p);
   QP_CUDA(c, cudaMemcpyAsync(pt2, d_pt2.p, n_st * sizeof(double), cudaMemcpyDeviceToHost, st));
+  if (per_gen) {
+    std::vector<double> part((size_t)n_items * n_st);
+    QP_CUDA(c, cudaMemcpyAsync(part.data(), d_part.p, part.size() * sizeof(double), cudaMemcpyDeviceToHost, st));
+    QP_CUDA(c, cudaStreamSynchronize(st));
+    for (int l = 0; l < n_list; ++l)
+      for (int s = 0; s < n_st; ++s) {
+        double acc = 0.0;
+        for (int64_t i = item_first[l]; i < item_first[l + 1]; ++i) acc += part[(size_t)i * n_st + s];
+        per_gen[(size_t)l * n_st + s] = acc;
+      }
+  }
   if (n_ext) *n_ext = (int64_t)hcnt[0];
-  const uint64_t nc = hcnt[1];
+  const uint64_t nc = std::min<uint64_t>(hcnt[1], cap);
   int nout = (int)std::min<uint64_t>(nc, (uint64_t)buf_size);
   if (nout > 0) {
     // sort by value on the device; the head (and any tie group crossing its
@@ -731,4 +759,38 @@ extern "C" int qpgpu_select_pt2(qpgpu_ctx* c, const double* coef, int n_st, cons
   }
   QP_CUDA(c, cudaStreamSynchronize(st));
   return nout;
+}
+
+extern "C" int qpgpu_select_pt2(qpgpu_ctx* c, const double* coef, int n_st, const double* e0, int n_gen, int n_sel,
+                                int buf_size, double* pt2, uint64_t* buf_dets, double* buf_vals, int64_t* n_ext) {
+  if (!c) return QPGPU_ERR_ARG;
+  if (!coef || !e0 || !pt2 || n_st < 1 || n_st > SEL_MAXST || buf_size < 0 ||
+      (buf_size > 0 && (!buf_dets || !buf_vals)))
+    return qpgpu_fail(c, QPGPU_ERR_ARG, "select_pt2: bad arguments (1 <= n_st <= 8, buffers for buf_size > 0)");
+  std::lock_guard<std::mutex> lk(c->mu);
+  if (!c->have_ints || !c->have_dets)
+    return qpgpu_fail(c, QPGPU_ERR_STATE, "select_pt2: integrals and determinants first");
+  if (n_gen < 1 || n_gen > n_sel || n_sel > c->N)
+    return qpgpu_fail(c, QPGPU_ERR_ARG, "select_pt2: need 1 <= n_gen <= n_sel <= N_det");
+  std::vector<int> gens(n_gen);
+  for (int g = 0; g < n_gen; ++g) gens[g] = g;
+  return run_selection(c, coef, n_st, e0, n_sel, gens, buf_size, pt2, nullptr, buf_dets, buf_vals, n_ext);
+}
+
+extern "C" int qpgpu_pt2_generators(qpgpu_ctx* c, const double* coef, int n_st, const double* e0, int n_sel,
+                                    const int32_t* gens, int n_list, double* pt2_detail) {
+  if (!c) return QPGPU_ERR_ARG;
+  if (!coef || !e0 || !gens || !pt2_detail || n_st < 1 || n_st > SEL_MAXST || n_list < 0)
+    return qpgpu_fail(c, QPGPU_ERR_ARG, "pt2_generators: bad arguments (1 <= n_st <= 8)");
+  std::lock_guard<std::mutex> lk(c->mu);
+  if (!c->have_ints || !c->have_dets)
+    return qpgpu_fail(c, QPGPU_ERR_STATE, "pt2_generators: integrals and determinants first");
+  if (n_sel < 1 || n_sel > c->N) return qpgpu_fail(c, QPGPU_ERR_ARG, "pt2_generators: need 1 <= n_sel <= N_det");
+  std::vector<int> g(gens, gens + n_list);
+  for (int x : g)
+    if (x < 0 || x >= n_sel) return qpgpu_fail(c, QPGPU_ERR_ARG, "pt2_generators: generator outside 0..n_sel-1");
+  if (n_list == 0) return QPGPU_OK;
+  std::vector<double> tot(n_st);
+  const int rc = run_selection(c, coef, n_st, e0, n_sel, g, 0, tot.data(), pt2_detail, nullptr, nullptr, nullptr);
+  return rc < 0 ? rc : QPGPU_OK;
 }

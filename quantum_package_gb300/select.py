@@ -60,3 +60,46 @@ def select(make_wf, dets, coefs, e0, buf_size, threshold_generators=0.99, thresh
     finally:
         wf.close()
     return dict(pt2=pt2, dets=bd, vals=bv, n_ext=n_ext, n_gen=n_gen, n_sel=n_sel, order=order)
+
+
+def pt2_stochastic(make_wf, dets, coefs, e0, relative_error=1e-3, absolute_error=0.0, seed=0, batch=256,
+                   threshold_generators=0.99, threshold_selectors=0.999):
+    """ZMQ_pt2 over the wave function (dets, coefs [N][n_st]): the comb
+    estimate of every state's second-order energy with its error.  As the
+    reference, each state gets its own psi_det_sorted (state_average_weight
+    set to that state alone), hence its own generators and selectors.
+    Below max(10, n_st) determinants the full selection gives the exact sum.
+    The per-generator contributions are computed on the device in batches.
+    Returns dict(pt2, error, n_computed, n_combs, n_gen, n_sel) with
+    per-state lists."""
+    from . import pt2 as _pt2
+    coefs = np.asarray(coefs, dtype=np.float64).reshape(len(dets), -1)
+    n_st = coefs.shape[1]
+    e0 = np.asarray(e0, dtype=np.float64)
+    if len(dets) < max(10, n_st):
+        r = select(make_wf, dets, coefs, e0, 0, threshold_generators, threshold_selectors)
+        return dict(pt2=r["pt2"], error=np.zeros(n_st), n_computed=[r["n_gen"]] * n_st, n_combs=[0] * n_st,
+                    n_gen=[r["n_gen"]] * n_st, n_sel=[r["n_sel"]] * n_st)
+    out = dict(pt2=np.zeros(n_st), error=np.zeros(n_st), n_computed=[], n_combs=[], n_gen=[], n_sel=[])
+    for st in range(n_st):
+        w = np.zeros(n_st)
+        w[st] = 1.0
+        order = _ezfio.sorted_order(coefs, w)
+        contrib = _ezfio.average_norm_contrib(coefs, w)[order]
+        n_gen = n_det_generators(contrib, threshold_generators)
+        n_sel = n_det_selectors(contrib, n_gen, threshold_selectors, threshold_generators)
+        cs = np.ascontiguousarray(coefs[order])
+        wf = make_wf(np.ascontiguousarray(np.asarray(dets)[order]))
+        try:
+            r = _pt2.pt2_stochastic(lambda g: wf.pt2_generators(cs.T, e0, n_sel, g)[:, st:st + 1],
+                                    cs[:n_gen, st], n_det=len(dets), relative_error=relative_error,
+                                    absolute_error=absolute_error, seed=seed + st, batch=batch)
+        finally:
+            wf.close()
+        out["pt2"][st] = r["pt2"][0]
+        out["error"][st] = r["error"][0]
+        for k in ("n_computed", "n_combs"):
+            out[k].append(r[k])
+        out["n_gen"].append(n_gen)
+        out["n_sel"].append(n_sel)
+    return out

@@ -188,6 +188,18 @@ class Wavefunction:
             check(rc, self._ctx)
         return pt2, bd[:rc].copy(), bv[:rc].copy(), n_ext.value
 
+    def pt2_generators(self, coef, e0, n_sel, gens):
+        """pt2_detail (len(gens), n_st) of the listed generators
+        (qpgpu_pt2_generators); coef (n_st, N) sorted, gens 0-based."""
+        cm = np.ascontiguousarray(np.atleast_2d(coef), dtype=np.float64)
+        n_st = cm.shape[0]
+        e0 = np.ascontiguousarray(np.atleast_1d(e0), dtype=np.float64)
+        g = np.ascontiguousarray(np.asarray(gens), dtype=np.int32)
+        out = np.zeros((max(len(g), 1), n_st))
+        check(_lib.load().qpgpu_pt2_generators(self._ctx, _p(cm), n_st, _p(e0), int(n_sel), _p(g), len(g), _p(out)),
+              self._ctx)
+        return out[:len(g)]
+
     # --- dressing (MRCC / MRCEPA0) ---------------------------------------
     def set_dressing(self, idx_ref, idx_non_ref, delta_ij, delta_ij_s2, delta_ii=None):
         """Dressing of one state (delta_ij(istate,:,:) of the reference's providers):
