@@ -58,8 +58,8 @@
 namespace {
 
 constexpr int SBLK = 256;
-constexpr int SEL_TILE = 16384;    // FP64 numerators per CTA (128 KB of shared memory)
-constexpr int SEL_DTILE = 512;     // selectors staged per filtering pass
+constexpr int SEL_TILE = 16384;    // FP64 numerators per CTA at most (128 KB of shared memory)
+constexpr int SEL_DTILE = 256;     // selectors staged per filtering pass
 constexpr int SEL_MAXST = 8;       // states
 constexpr int SEL_MAXFG = 2048;    // earlier generators kept per item (checked, not assumed)
 
@@ -288,7 +288,6 @@ __global__ void __launch_bounds__(SBLK) k_sel_items(SelArgs A) {
   __shared__ int nfg;
   __shared__ int wsum[SBLK / 32];
   __shared__ int nsel_s;
-  __shared__ double red[SBLK][SEL_MAXST];
   const SelItem it = A.items[blockIdx.x];
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   const int nst = A.n_st, n = A.t.n;
@@ -478,11 +477,14 @@ __global__ void __launch_bounds__(SBLK) k_sel_items(SelArgs A) {
     }
   }
   if (next) atomicAdd(A.n_ext, next);
-  for (int s = 0; s < nst; ++s) red[tid][s] = pt[s];
+  // the numerator tile is free now: it holds the per-thread sums (the
+  // dynamic allocation is at least SBLK x n_st doubles)
+  __syncthreads();
+  for (int s = 0; s < nst; ++s) tile[tid * nst + s] = pt[s];
   __syncthreads();
   if (tid < nst) {
     double acc = 0.0;
-    for (int x = 0; x < SBLK; ++x) acc += red[x][tid];
+    for (int x = 0; x < SBLK; ++x) acc += tile[x * nst + tid];
     A.pt2_part[(int64_t)blockIdx.x * nst + tid] = acc;
   }
 }
@@ -658,7 +660,11 @@ static int run_selection(qpgpu_ctx* c, const double* coef, int n_st, const doubl
   A.n_ext = (unsigned long long*)d_cnt.p;
   A.n_cand = (unsigned long long*)d_cnt.p + 1;
   A.err = (int*)d_err.p;
-  const size_t smem = (size_t)SEL_TILE * sizeof(double);
+  // dynamic shared memory: the largest item's numerator tile (at least the
+  // SBLK x n_st doubles of the final reduction), so that several CTAs fit an SM
+  int max_ne = 0;
+  for (const SelItem& it : items) max_ne = std::max(max_ne, it.e1 - it.e0);
+  const size_t smem = (size_t)std::max(max_ne * n_st, SBLK * n_st) * sizeof(double);
   unsigned long long hcnt[2] = {0, 0};
   for (int attempt = 0; attempt < 2; ++attempt) {
     dev_free(d_cval.p);
