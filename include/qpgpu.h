@@ -331,6 +331,23 @@ int qpgpu_connected_pairs(qpgpu_ctx* ctx, int64_t* n_pairs, int32_t* I, int32_t*
 int qpgpu_connected_pairs_rows(qpgpu_ctx* ctx, const int32_t* rows, int64_t n_rows, int64_t* n_pairs, int32_t* I,
                                int32_t* J, int8_t* cls, int8_t* phase, int16_t* exc, double* hij, int64_t cap);
 
+/* O = [A_0 .. A_nb-1] C for tall blocks A_b (N x nsd, rows nsd doubles
+ * apart, blocks sA doubles apart; m = nb nsd) and C (m x nsd, row-major),
+ * device arrays, computed to FP64 accuracy on the tensor cores.  These are
+ * the Davidson's linear combinations: the Ritz vectors and the re-contraction
+ * (src/Davidson/diagonalization_hs2.irp.f:376-381,419-420, dgemm('N','N'))
+ * and the Gram-Schmidt updates.  Each row of A gets the exponent of its
+ * largest value and each column of C its own; the digit products are summed
+ * exactly, as in qpgpu_gram_tc.  The error of an entry is within a few
+ * 2^-56 of max|a_r| max|c_j| (norm-wise, at or below FP64's rounding of the
+ * largest product); an entry far below that scale has a larger relative
+ * error than an FP64 dot product would give it.  O (rows ldO doubles apart)
+ * may be the last block of A.  m <= 128, nsd <= 16.  The call waits for the stream (NULL:
+ * the context's); a bounded tensor-core wait that runs out gives
+ * QPGPU_ERR_TIMEOUT. */
+int qpgpu_lincomb_tc(qpgpu_ctx* ctx, const double* A, int64_t sA, int m, int nsd, const double* C, double* O,
+                     int64_t ldO, int64_t N, void* stream);
+
 /* CIPSI selection with the Epstein-Nesbet second-order energy over the
  * context's wave function, which must be in psi_det_sorted order: the
  * generators are determinants 0..n_gen-1 and the selectors 0..n_sel-1

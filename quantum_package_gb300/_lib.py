@@ -100,6 +100,7 @@ def load():
         "qpgpu_select_pt2": (C.c_int, [vp, vp, C.c_int, vp, C.c_int, C.c_int, C.c_int, vp, vp, vp,
                                        C.POINTER(C.c_int64)]),
         "qpgpu_pt2_generators": (C.c_int, [vp, vp, C.c_int, vp, C.c_int, vp, C.c_int, vp]),
+        "qpgpu_lincomb_tc": (C.c_int, [vp, vp, C.c_int64, C.c_int, C.c_int, vp, vp, C.c_int64, C.c_int64, vp]),
         "qpgpu_batch_create": (C.c_int, [vp, C.c_int, C.POINTER(vp)]),
         "qpgpu_batch_destroy": (C.c_int, [vp]),
         "qpgpu_batch_last_error": (C.c_char_p, [vp]),

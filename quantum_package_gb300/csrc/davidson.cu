@@ -1084,6 +1084,20 @@ void gram_tc(Dav& d, const double* A, int m, const double* B0, const double* B1,
   qp_oz_reduce(d.part, d.c->n_sm, m * nbc, out, skip, d.st);
 }
 
+// lincomb on the tensor cores (FP64-accurate Ozaki splitting, ozaki.cu), one
+// (A, out) pair after the other; shapes outside the kernel's range (m > 128)
+// take the FP64 pipe
+void lincomb(Dav& d, int m, const double* C, const double* A0, double* O0, const double* A1, double* O1,
+             const double* A2, double* O2, const int* skip);
+void lincomb_tc(Dav& d, int m, const double* C, const double* A0, double* O0, const double* A1 = nullptr,
+                double* O1 = nullptr, const double* A2 = nullptr, double* O2 = nullptr, const int* skip = nullptr) {
+  const double* A[3] = {A0, A1, A2};
+  double* O[3] = {O0, O1, O2};
+  for (int t = 0; t < 3 && A[t]; ++t)
+    if (qp_lincomb_oz(A[t], d.N * d.nsd, m, d.nsd, C, O[t], d.nsd, d.N, d.c->n_sm, skip, d.bexp + 2 * MAXS, d.st))
+      lincomb(d, m, C, A[t], O[t], nullptr, nullptr, nullptr, nullptr, skip);
+}
+
 // float-float copy of one block (X1 = nullptr) or of [X0 X1]
 void split_block(Dav& d, const double* X0, const double* X1, float2* out, const int* skip = nullptr) {
   const int nx = X1 ? 2 : 1;
@@ -1249,17 +1263,19 @@ void orthonormalise(Dav& d, int b, bool ff) {
   double* Rinv = d.small + OFF_RINV;
   int* skip2 = (int*)(d.small + OFF_FLAG);
   const int m = b * d.nsd, m1 = m + d.nsd;
-  if (d.tc) {  // Gram blocks on the tensor cores, updates in FP64
+  if (d.tc) {  // Gram blocks and updates on the tensor cores (FP64-accurate)
     if (b > 0) {
       gram_tc(d, d.U, m1, Ub, nullptr, X, TC_BASIS_NEW);
       k_cgs_coef<<<1, 128, 0, d.st>>>(X, m, d.nsd, K, skip2, 0);
-      lincomb(d, m1, K, d.U, Ub);
+      lincomb_tc(d, m1, K, d.U, Ub);
       gram_tc(d, d.U, m1, Ub, nullptr, X, TC_BASIS_NEW, skip2);
       k_cgs_coef<<<1, 128, 0, d.st>>>(X, m, d.nsd, K, skip2, 1);
-      lincomb(d, m1, K, d.U, Ub, nullptr, nullptr, nullptr, nullptr, skip2);
+      lincomb_tc(d, m1, K, d.U, Ub, nullptr, nullptr, nullptr, nullptr, skip2);
     }
+    // the nsd x nsd self-Gram and update of Cholesky-QR are too small for
+    // the tensor cores' fixed cost: they stay on the FP64 pipe
     for (int pass = (b > 0) ? 1 : 0; pass < 2; ++pass) {
-      gram_tc(d, Ub, d.nsd, Ub, nullptr, G, TC_SELF);
+      gram(d, Ub, d.nsd, Ub, nullptr, G);
       k_chol_inv<<<1, 32, 0, d.st>>>(G, d.nsd, Rinv);
       lincomb(d, d.nsd, Rinv, Ub, Ub);
     }
@@ -1603,6 +1619,8 @@ extern "C" int qpgpu_davidson_hs2(qpgpu_ctx* c, double* u_in, int64_t dim_in, do
         lincomb32(d, shift2, ydev, d.U, d.blk(d.U, iter), d.W, d.blk(d.W, iter), d.S, d.blk(d.S, iter));
       else if (ffalg)  // restart iteration: float-float
         lincomb_ff(d, shift2, ydev, d.U, d.blk(d.U, iter), d.W, d.blk(d.W, iter), d.S, d.blk(d.S, iter));
+      else if (tcalg)
+        lincomb_tc(d, shift2, ydev, d.U, d.blk(d.U, iter), d.W, d.blk(d.W, iter), d.S, d.blk(d.S, iter));
       else
         lincomb(d, shift2, ydev, d.U, d.blk(d.U, iter), d.W, d.blk(d.W, iter), d.S, d.blk(d.S, iter));
       prof.mark(DavProf::RITZ);
@@ -1692,6 +1710,8 @@ extern "C" int qpgpu_davidson_hs2(qpgpu_ctx* c, double* u_in, int64_t dim_in, do
     QP_CUDA(c, cudaMemcpyAsync(ydev, ycoef.data(), ycoef.size() * sizeof(double), cudaMemcpyHostToDevice, st));
     if (ffalg)
       lincomb_ff(d, shift2, ydev, d.U, d.R);
+    else if (tcalg)
+      lincomb_tc(d, shift2, ydev, d.U, d.R);
     else
       lincomb(d, shift2, ydev, d.U, d.R);
     k_copy<<<gsz((int64_t)blkn), DBLK, 0, st>>>(d.R, d.U, (int64_t)blkn);

@@ -502,6 +502,276 @@ __global__ void __launch_bounds__(OZ_THREADS, 1) k_gram_oz(OzArgs g) {
     asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(OZ_TMEM_COLS));
 }
 
+
+// ---- linear combinations O = [A_0 .. A_nb-1] C on the tensor cores --------
+//
+// O(r, j) = sum_i A(r, i) C(i, j): the Davidson updates (Gram-Schmidt and
+// Cholesky-QR, Ritz vectors, re-contraction).  A is nb blocks of nsd columns
+// (rows nsd doubles apart, blocks sA apart), C is (m x nsd) row-major
+// (m = nb nsd), O has rows ldO doubles apart and may be the last block of A.
+// The contraction runs over i, so each row r of A gets its own exponent
+// (the largest over its m values) and C one per column j; the digits and
+// levels are those of k_gram_oz, and a level of one entry sums at most
+// m <= 128 products, below 2^23.  One CTA per SM walks tiles of 128 rows:
+// the tile's rows are loaded into shared memory, its row exponents formed,
+// then each K step of 16 columns is cut into the 8 A digit planes (two
+// stages, so that the split of step c + 1 overlaps the MMAs of step c) and
+// one thread issues its 8 MMAs (M = 128 rows, N = (8 - p) 16, K = 16) into
+// the tile's accumulator; when the tile's MMAs are done, warps 0-3 read the
+// 8 levels of their rows and write O in FP64.  The digit planes of C are
+// built once per CTA.  Waits are bounded as in k_gram_oz.
+constexpr int LC_THREADS = 512;             // 16 warps: 4 threads per row of a tile
+constexpr int LC_RQ = LC_THREADS / 128;      // threads per row
+constexpr int LC_TM = 128;                       // rows per tile (MMA M)
+constexpr int LC_KS = 16;                        // K step (columns of A)
+constexpr int LC_APLANE = LC_TM * LC_KS * 2;     // 4 KB: one A digit plane of one K step
+constexpr int LC_ASTAGE = OZ_DIG * LC_APLANE;    // 32 KB
+constexpr int LC_BCHUNK = OZ_DIG * OZ_N * LC_KS * 2;  // 4 KB: the 8 C planes of one K step
+constexpr int LC_MAXM = 128;
+constexpr int LC_TMEM_COLS = OZ_LEVELS * OZ_N;   // 128
+
+struct LcArgs {
+  const double* A;
+  int64_t sA;
+  int m, nsd;
+  const double* C;  // (m, nsd) row-major
+  double* O;
+  int64_t ldO;
+  int64_t N, rows_per_cta;
+  int row_stride;  // doubles per staged row in shared memory
+  const int* skip;
+  int* status;
+};
+
+// byte offset of (row, k) in a K-major tile of 8 x 16-byte core matrices
+// with K = 16: row-group stride (SBO) 256 bytes, K-direction stride (LBO) 128
+__device__ __forceinline__ int kmaj16(int row, int k) {
+  return (((row >> 3) * 2) + (k >> 3)) * 128 + (row & 7) * 16 + (k & 7) * 2;
+}
+__device__ __forceinline__ uint64_t sdesc16(uint32_t addr) {
+  return (uint64_t)((addr & 0x3FFFF) >> 4) | ((uint64_t)(128 >> 4) << 16) | ((uint64_t)(256 >> 4) << 32) |
+         ((uint64_t)1 << 46);
+}
+
+__device__ __forceinline__ int biased_exp(double x) {
+  return (int)(((unsigned long long)__double_as_longlong(x) >> 52) & 0x7FF);
+}
+
+__global__ void __launch_bounds__(LC_THREADS, 1) k_lincomb_oz(LcArgs g) {
+  if (g.skip && *g.skip) return;
+  extern __shared__ __align__(1024) uint8_t smem[];
+  uint8_t* sbase = (uint8_t*)(((uintptr_t)smem + 1023) & ~(uintptr_t)1023);
+  uint8_t* adig = sbase;                                  // 2 stages of 8 A planes
+  uint8_t* bdig = sbase + 2 * LC_ASTAGE;                  // nks x 8 C planes
+  const int m = g.m, nsd = g.nsd, nb = m / nsd;
+  const int nks = (m + LC_KS - 1) / LC_KS;
+  const int rs = g.row_stride;                            // doubles per staged row (nsd, or nsd + 1: odd)
+  double* raw = (double*)(bdig + (size_t)nks * LC_BCHUNK);  // [block][128 rows][rs]
+  int* eb = (int*)(raw + (size_t)nb * LC_TM * rs);        // [128] row exponents
+  int* ej = eb + LC_TM;                                    // [16] column exponents of C
+  // [LC_RQ][128] partial row exponents: in digit stage 1, idle at the start
+  // of a tile (the previous tile's MMAs are done, its flush used stage 0)
+  int* eh = (int*)(adig + LC_ASTAGE);
+  uint64_t* bars = (uint64_t*)(((uintptr_t)(ej + OZ_N) + 7) & ~(uintptr_t)7);  // stage[2], tile
+  uint32_t* tmem_slot = (uint32_t*)(bars + 3);
+  int* sflag = (int*)(tmem_slot + 1);
+  const int tid = threadIdx.x, warp = tid >> 5;
+  const uint32_t bar0 = smem_u32(bars);
+
+  if (warp == 0) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(tmem_slot)),
+                 "r"(LC_TMEM_COLS));
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
+  }
+  if (tid == 0) {
+    for (int b = 0; b < 3; ++b) asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(bar0 + 8u * b));
+    asm volatile("fence.mbarrier_init.release.cluster;");
+    *sflag = 0;
+  }
+  // C: column exponents, then its digit planes (rows j of plane q at q 16 + j)
+  for (int x = tid; x < nks * LC_BCHUNK / 16; x += LC_THREADS) reinterpret_cast<uint4*>(bdig)[x] = make_uint4(0, 0, 0, 0);
+  if (tid < OZ_N) {
+    int e = 0;
+    if (tid < nsd)
+      for (int i = 0; i < m; ++i) e = max(e, biased_exp(g.C[(int64_t)i * nsd + tid]));
+    ej[tid] = e;
+  }
+  __syncthreads();
+  for (int x = tid; x < m * nsd; x += LC_THREADS) {
+    const int i = x / nsd, j = x - i * nsd;
+    float d[OZ_DIG];
+    oz_digits(g.C[x], ej[j], d);
+    uint8_t* base = bdig + (size_t)(i / LC_KS) * LC_BCHUNK;
+    const int k = i % LC_KS;
+#pragma unroll
+    for (int q = 0; q < OZ_DIG; ++q)
+      *reinterpret_cast<uint16_t*>(base + kmaj16(q * OZ_N + j, k)) = (uint16_t)(__float_as_uint(d[q]) >> 16);
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;");
+  __syncthreads();
+  asm volatile("tcgen05.fence::after_thread_sync;");
+  const uint32_t tmem = *tmem_slot;
+
+  const int64_t r0 = (int64_t)blockIdx.x * g.rows_per_cta;
+  const int64_t r1 = min(r0 + g.rows_per_cta, g.N);
+  const int ntile = r1 > r0 ? (int)((r1 - r0 + LC_TM - 1) / LC_TM) : 0;
+  int gstep = 0;            // K steps issued so far (stage = gstep & 1)
+  bool ok = true;
+  uint32_t last_bar = 0, last_par = 0;
+  // tile tt's rows into the padded staging rows with asynchronous 8-byte
+  // copies: thread (row r, quarter h) copies blocks h, h + 4, ... of its row
+  auto issue_rows = [&](int tt) {
+    const int64_t Rt = r0 + (int64_t)tt * LC_TM;
+    const int nrt = (int)min((int64_t)LC_TM, r1 - Rt);
+    const int r = tid & (LC_TM - 1), h = tid >> 7;
+    if (r < nrt)
+      for (int b = h; b < nb; b += LC_RQ) {
+        const double* src = g.A + (int64_t)b * g.sA + (Rt + r) * nsd;
+        const uint32_t dst = smem_u32(raw + ((size_t)b * LC_TM + r) * rs);
+        for (int c = 0; c < nsd; ++c)
+          asm volatile("cp.async.ca.shared.global [%0], [%1], 8;" ::"r"(dst + 8u * c), "l"(src + c) : "memory");
+      }
+    asm volatile("cp.async.commit_group;" ::: "memory");
+  };
+  if (ntile > 0) issue_rows(0);
+  for (int t = 0; t < ntile && ok; ++t) {
+    const int64_t R = r0 + (int64_t)t * LC_TM;
+    const int nr = (int)min((int64_t)LC_TM, r1 - R);
+    // this tile's rows have landed: their largest exponents
+    asm volatile("cp.async.wait_group 0;" ::: "memory");
+    __syncthreads();
+    {
+      const int r = tid & (LC_TM - 1), h = tid >> 7;
+      int e = 0;
+      if (r < nr)
+        for (int b = h; b < nb; b += LC_RQ) {
+          const double* row = raw + ((size_t)b * LC_TM + r) * rs;
+          for (int c = 0; c < nsd; ++c) e = max(e, biased_exp(row[c]));
+        }
+      eh[h * LC_TM + r] = e;
+    }
+    __syncthreads();
+    if (tid < LC_TM) eb[tid] = max(max(eh[tid], eh[LC_TM + tid]), max(eh[2 * LC_TM + tid], eh[3 * LC_TM + tid]));
+    __syncthreads();
+    for (int c = 0; c < nks; ++c, ++gstep) {
+      const int s = gstep & 1;
+      // the MMAs of step gstep - 2 are done with stage s
+      if (gstep >= 2 && !mbar_wait(bar0 + 8u * s, (uint32_t)((gstep >> 1) - 1) & 1u, sflag)) ok = false;
+      if (!__syncthreads_and(ok)) {
+        ok = false;
+        break;
+      }
+      uint8_t* sa = adig + s * LC_ASTAGE;
+      {
+        // thread: row r, 4 consecutive K of the step (half a 16-byte core row per plane)
+        const int r = tid & (LC_TM - 1), k0 = (tid >> 7) * 4;
+        const int er = eb[r];
+        // column i of A is (block bi, column si) of the staged rows
+        const int ibeg = c * LC_KS + k0;
+        int bi = ibeg / nsd, si = ibeg - bi * nsd;
+        double xv[4];
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+          xv[k] = (r < nr && ibeg + k < m) ? raw[((size_t)bi * LC_TM + r) * rs + si] : 0.0;
+          if (++si == nsd) {
+            si = 0;
+            ++bi;
+          }
+        }
+        uint32_t pk[OZ_DIG][2];
+#pragma unroll
+        for (int k = 0; k < 4; k += 2) {
+          float d0[OZ_DIG], d1[OZ_DIG];
+          oz_digits(xv[k], er, d0);
+          oz_digits(xv[k + 1], er, d1);
+#pragma unroll
+          for (int p = 0; p < OZ_DIG; ++p) pk[p][k >> 1] = bf16x2(d0[p], d1[p]);
+        }
+#pragma unroll
+        for (int p = 0; p < OZ_DIG; ++p)
+          *reinterpret_cast<uint2*>(sa + p * LC_APLANE + kmaj16(r, k0)) = make_uint2(pk[p][0], pk[p][1]);
+      }
+      asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+      __syncthreads();
+      if (tid == 0) {
+        asm volatile("tcgen05.fence::after_thread_sync;");
+        const uint32_t a0 = smem_u32(sa), b0 = smem_u32(bdig + (size_t)c * LC_BCHUNK);
+#pragma unroll
+        for (int p = 0; p < OZ_DIG; ++p) {
+          const uint32_t acc = (c == 0 && p == 0) ? 0u : 1u;
+          asm volatile(
+              "{\n .reg .pred pa;\n setp.ne.b32 pa, %4, 0;\n"
+              " tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, pa;\n}" ::"r"(tmem + (uint32_t)(p * OZ_N)),
+              "l"(sdesc16(a0 + p * LC_APLANE)), "l"(sdesc16(b0)), "r"(oz_idesc((OZ_LEVELS - p) * OZ_N)), "r"(acc));
+        }
+        mma_commit(bar0 + 8u * s);
+        last_bar = bar0 + 8u * s;
+        last_par = (uint32_t)(gstep >> 1) & 1u;
+      }
+    }
+    if (!ok) break;
+    // every split of this tile is done, so the staging rows are free: the
+    // next tile's copies fly during this tile's MMA tail and flush
+    if (t + 1 < ntile) issue_rows(t + 1);
+    // the tile's MMAs are done: warps 0-3 write its rows
+    if (tid == 0) mma_commit(bar0 + 16u);
+    if (!mbar_wait(bar0 + 16u, (uint32_t)t & 1u, sflag)) ok = false;
+    if (!__syncthreads_and(ok)) {
+      ok = false;
+      break;
+    }
+    asm volatile("tcgen05.fence::after_thread_sync;");
+    {
+      // warps w and w + 4 share lane quarter w % 4 (rows 32 (w % 4) ..):
+      // warp w sums levels 0-3, warp w + 4 levels 4-7; both halves meet in
+      // shared memory (the digit stages are free now)
+      long long acc[OZ_N];
+#pragma unroll
+      for (int j = 0; j < OZ_N; ++j) acc[j] = 0;
+      const uint32_t ta = tmem + ((uint32_t)((warp & 3) * 32) << 16);
+      if (warp < 4) {
+#pragma unroll
+        for (int L = 0; L < OZ_LEVELS / 2; ++L) oz_flush1(ta + L * OZ_N, 7 * (3 - L), acc);
+      } else if (warp < 8) {
+#pragma unroll
+        for (int L = OZ_LEVELS / 2; L < OZ_LEVELS; ++L) oz_flush1(ta + L * OZ_N, 7 * (7 - L), acc);
+      }
+      long long* lo_s = reinterpret_cast<long long*>(adig);  // [128 rows][17]: odd stride, no bank conflicts
+      const int r = tid & (LC_TM - 1);
+      if (warp >= 4 && warp < 8)
+#pragma unroll
+        for (int j = 0; j < OZ_N; ++j) lo_s[r * (OZ_N + 1) + j] = acc[j];
+      __syncthreads();
+      if (warp < 4 && r < nr) {
+        double* o = g.O + (R + r) * g.ldO;
+#pragma unroll
+        for (int j = 0; j < OZ_N; ++j)
+          if (j < nsd) {
+            const int e = (eb[r] - 1022) + (ej[j] - 1022);
+            const double h = (double)acc[j], l = (double)lo_s[r * (OZ_N + 1) + j];
+            double v;
+            if (e - 63 >= -1022 && e - 35 <= 1023)  // both scales are normal powers of two: exact products
+              v = h * __longlong_as_double((long long)(e - 35 + 1023) << 52) +
+                  l * __longlong_as_double((long long)(e - 63 + 1023) << 52);
+            else
+              v = ldexp(h, e - 35) + ldexp(l, e - 63);
+            o[j] = v;
+          }
+      }
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;");
+    __syncthreads();
+  }
+  // no copy or MMA may be in flight when the CTA exits / frees its tensor memory
+  asm volatile("cp.async.wait_group 0;" ::: "memory");
+  if (tid == 0 && last_bar != 0 && !mbar_drain(last_bar, last_par)) atomicExch(sflag, 1);
+  asm volatile("tcgen05.fence::before_thread_sync;");
+  __syncthreads();
+  asm volatile("tcgen05.fence::after_thread_sync;");
+  if (tid == 0 && (!ok || *(volatile int*)sflag)) atomicExch(g.status, 1);
+  if (warp == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(LC_TMEM_COLS));
+}
+
 // biased max exponent of each column (nsd <= 256 columns per block, rows ld
 // values apart, nblk blocks sX apart) into E[col0 + block * nsd + s]
 // (atomicMax; E must be zeroed first).  Thread t of a CTA keeps column
@@ -614,6 +884,57 @@ void qp_gram_oz(const double* A, int64_t sA, int m, int nsdA, int ldA, const dou
   k_gram_oz<<<ncta, OZ_THREADS, smem, st>>>(g);
 }
 
+
+// Opt-in shared memory of k_lincomb_oz (once per device).
+static int lincomb_oz_prepare() {
+  static int done[64] = {0};
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return -1;
+  if (done[dev]) return 0;
+  if (cudaFuncSetAttribute(k_lincomb_oz, cudaFuncAttributeMaxDynamicSharedMemorySize, OZ_SMEM_MAX) != cudaSuccess)
+    return -1;
+  done[dev] = 1;
+  return 0;
+}
+
+// O = [A_0 .. A_nb-1] C on the tensor cores (FP64-accurate); m = nb nsd <=
+// 128, nsd <= 16.  Returns -1 when the shapes are outside the kernel's range
+// (the caller keeps its FP64 path), else 0.
+int qp_lincomb_oz(const double* A, int64_t sA, int m, int nsd, const double* C, double* O, int64_t ldO, int64_t N,
+                  int ncta, const int* skip, int* status, cudaStream_t st) {
+  if (m < 1 || m > LC_MAXM || nsd < 1 || nsd > OZ_N || m % nsd) return -1;
+  if (lincomb_oz_prepare()) return -1;
+  const int nks = (m + LC_KS - 1) / LC_KS;
+  const int nb = m / nsd;
+  // staged rows of an odd number of doubles (no shared-memory bank
+  // conflicts between consecutive rows) when they fit, else unpadded
+  auto need = [&](int rsd) {
+    return 1024 + 2 * (size_t)LC_ASTAGE + (size_t)nks * LC_BCHUNK + (size_t)nb * LC_TM * rsd * 8 +
+           (LC_TM + OZ_N) * 4 + 64;
+  };
+  int rsd = (nsd & 1) ? nsd : nsd + 1;
+  if (need(rsd) > (size_t)OZ_SMEM_MAX) rsd = nsd;
+  const size_t smem = need(rsd);
+  if (smem > (size_t)OZ_SMEM_MAX) return -1;
+  LcArgs g;
+  g.A = A;
+  g.sA = sA;
+  g.m = m;
+  g.nsd = nsd;
+  g.C = C;
+  g.O = O;
+  g.ldO = ldO;
+  g.N = N;
+  int64_t rpc = (N + ncta - 1) / ncta;
+  rpc = (rpc + LC_TM - 1) / LC_TM * LC_TM;
+  g.rows_per_cta = rpc;
+  g.row_stride = rsd;
+  g.skip = skip;
+  g.status = status;
+  k_lincomb_oz<<<ncta, LC_THREADS, smem, st>>>(g);
+  return 0;
+}
+
 extern "C" int qpgpu_gram_tc(qpgpu_ctx* c, const double* A, int64_t lda, int m, const double* B, int64_t ldb, int n,
                              int64_t N, double* X, void* stream) {
   if (!c) return QPGPU_ERR_ARG;
@@ -644,5 +965,32 @@ extern "C" int qpgpu_gram_tc(qpgpu_ctx* c, const double* A, int64_t lda, int m, 
   QP_CUDA(c, cudaMemcpyAsync(&hs, status, sizeof(int), cudaMemcpyDeviceToHost, st));
   QP_CUDA(c, cudaStreamSynchronize(st));
   if (hs) return qpgpu_fail(c, QPGPU_ERR_TIMEOUT, "gram_tc: a bounded tensor-core wait ran out");
+  return QPGPU_OK;
+}
+
+extern "C" int qpgpu_lincomb_tc(qpgpu_ctx* c, const double* A, int64_t sA, int m, int nsd, const double* C, double* O,
+                                int64_t ldO, int64_t N, void* stream) {
+  if (!c) return QPGPU_ERR_ARG;
+  if (!A || !C || !O || m < 1 || m > LC_MAXM || nsd < 1 || nsd > OZ_N || m % nsd || N < 1 || ldO < nsd ||
+      (m > nsd && sA < N * nsd))
+    return qpgpu_fail(c, QPGPU_ERR_ARG, "lincomb_tc: need m = nb nsd <= 128, nsd <= 16, N >= 1, ldO >= nsd, sA >= N nsd");
+  std::lock_guard<std::mutex> lk(c->mu);
+  if (!c->d_tc_scratch || c->tc_scratch_bytes < sizeof(int)) {
+    dev_free(c->d_tc_scratch);
+    c->d_tc_scratch = nullptr;
+    c->tc_scratch_bytes = 0;
+    QP_CUDA(c, cudaMalloc(&c->d_tc_scratch, 256));
+    c->tc_scratch_bytes = 256;
+  }
+  int* status = (int*)c->d_tc_scratch;
+  cudaStream_t st = stream ? (cudaStream_t)stream : c->stream;
+  QP_CUDA(c, cudaMemsetAsync(status, 0, sizeof(int), st));
+  if (qp_lincomb_oz(A, sA, m, nsd, C, O, ldO, N, c->n_sm, nullptr, status, st))
+    return qpgpu_fail(c, QPGPU_ERR_CUDA, "lincomb_tc: shared-memory opt-in failed");
+  QP_CUDA(c, cudaGetLastError());
+  int hs = 0;
+  QP_CUDA(c, cudaMemcpyAsync(&hs, status, sizeof(int), cudaMemcpyDeviceToHost, st));
+  QP_CUDA(c, cudaStreamSynchronize(st));
+  if (hs) return qpgpu_fail(c, QPGPU_ERR_TIMEOUT, "lincomb_tc: a bounded tensor-core wait ran out");
   return QPGPU_OK;
 }

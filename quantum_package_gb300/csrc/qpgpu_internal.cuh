@@ -516,6 +516,8 @@ void qp_free_dressing(qpgpu_ctx* c);
 
 // FP64-accurate Gram blocks on the tensor cores (ozaki.cu)
 int qp_gram_oz_prepare();
+int qp_lincomb_oz(const double* A, int64_t sA, int m, int nsd, const double* C, double* O, int64_t ldO, int64_t N,
+                  int ncta, const int* skip, int* status, cudaStream_t st);
 void qp_col_maxexp(const double* X, int nblk, int64_t sX, int nsd, int ld, int64_t N, int* E, int col0,
                    const int* skip, cudaStream_t st, int n_sm);
 void qp_gram_oz(const double* A, int64_t sA, int m, int nsdA, int ldA, const double* B0, const double* B1, int nbc,

@@ -97,3 +97,62 @@ def test_gram_tc_rejects_bad_shapes(wf):
     L = _lib.load()
     assert L.qpgpu_gram_tc(wf.ctx, C.c_void_p(8), 200, 129, C.c_void_p(8), 8, 8, 10, C.c_void_p(8), None) == -1
     assert L.qpgpu_gram_tc(wf.ctx, C.c_void_p(8), 4, 8, C.c_void_p(8), 8, 8, 10, C.c_void_p(8), None) == -1
+
+
+def _lincomb_tc(wf, blocks, Cm, out_is_last=False):
+    import torch
+    nb, N, nsd = blocks.shape
+    dA = torch.from_numpy(np.ascontiguousarray(blocks)).cuda()
+    dC = torch.from_numpy(np.ascontiguousarray(Cm)).cuda()
+    dO = dA[nb - 1] if out_is_last else torch.empty((N, nsd), dtype=torch.float64, device="cuda")
+    L = _lib.load()
+    rc = L.qpgpu_lincomb_tc(wf.ctx, C.c_void_p(dA.data_ptr()), N * nsd, nb * nsd, nsd, C.c_void_p(dC.data_ptr()),
+                            C.c_void_p(dO.data_ptr()), nsd, N, None)
+    _lib.check(rc, wf.ctx)
+    return dO.cpu().numpy()
+
+
+@pytest.mark.parametrize("N,nb,nsd", [(129, 1, 8), (5000, 10, 8), (300_017, 7, 6), (1_000_000, 10, 8), (4000, 16, 8)])
+def test_lincomb_tc_exact_sums(wf, N, nb, nsd):
+    # O = [A_0 .. A_nb-1] C (the Davidson's Ritz vectors / Gram-Schmidt
+    # updates).  Each row of A and each column of C has one scale (its
+    # largest exponent), so the bar is norm-wise: within
+    # 4 eps sqrt(m) max|a_r| max|c_j| of the exact value, the size of FP64's
+    # rounding of the largest product.  Component-wise bounds of an FP64 dot
+    # product are tighter for entries far below that scale.
+    rng = np.random.default_rng(N + nb)
+    blocks = rng.normal(size=(nb, N, nsd)) * np.exp(rng.uniform(-10, 0, size=(nb, N, nsd)))
+    Cm = rng.normal(size=(nb * nsd, nsd)) * np.exp(rng.uniform(-6, 0, size=(nb * nsd, nsd)))
+    Cm[:nsd] = np.eye(nsd)  # the identity part of a Gram-Schmidt update
+    O = _lincomb_tc(wf, blocks, Cm)
+    A = np.concatenate(list(blocks), axis=1)  # (N, m)
+    Od = A @ Cm
+    m = nb * nsd
+    rmax = np.abs(A).max(axis=1)
+    cmax = np.abs(Cm).max(axis=0)
+    errs = []
+    for r in rng.choice(N, 6):
+        for j in rng.choice(nsd, 2):
+            ex = _exact_dot(A[r], Cm[:, j])
+            bar = 4 * EPS * math.sqrt(m) * rmax[r] * cmax[j]
+            assert abs(O[r, j] - ex) <= bar, (r, j, O[r, j], ex)
+            errs.append(abs(O[r, j] - ex) / (rmax[r] * cmax[j]))
+    assert np.all(np.abs(O - Od) <= 16 * EPS * math.sqrt(m) * np.outer(rmax, cmax) + 1e-300)
+    print(f"\nN={N} m={m}: error / (max|a_r| max|c_j|) up to {max(errs):.1e}")
+
+
+def test_lincomb_tc_in_place_and_zeros(wf):
+    # the output may be the last block of A (the Gram-Schmidt update writes
+    # the new block in place); zero rows and zero columns of C give zeros
+    rng = np.random.default_rng(3)
+    N, nb, nsd = 70_001, 5, 8
+    blocks = rng.normal(size=(nb, N, nsd))
+    blocks[:, 17] = 0.0
+    Cm = rng.normal(size=(nb * nsd, nsd))
+    Cm[:, 3] = 0.0
+    ref = np.concatenate(list(blocks), axis=1) @ Cm
+    O = _lincomb_tc(wf, blocks, Cm, out_is_last=True)
+    np.testing.assert_allclose(O, ref, rtol=0, atol=1e-13 * np.abs(ref).max())
+    assert np.all(O[17] == 0.0) and np.all(O[:, 3] == 0.0)
+    L = _lib.load()
+    assert L.qpgpu_lincomb_tc(wf.ctx, None, 0, 0, 8, None, None, 8, 10, None) < 0
