@@ -213,11 +213,12 @@ typedef struct qpgpu_davidson_params {
   int32_t algebra;          /* QPGPU_ALGEBRA_FAST (mixed modes): projections, Gram-Schmidt, Ritz vectors
                                and the step on the FP32 pipes (float-float / FP32); QPGPU_ALGEBRA_FP64:
                                all of them in FP64 as in the plain loop, so only sigma runs in FP32;
-                               QPGPU_ALGEBRA_TC (any precision): FP64-accurate with the Gram blocks
-                               (projections, Gram-Schmidt and Cholesky-QR Grams) on the tensor cores
-                               (qpgpu_gram_tc's splitting), updates, step and residual norms in FP64,
-                               the Ritz vectors of FP32-sigma iterations in FP32 (they only feed the
-                               step) */
+                               QPGPU_ALGEBRA_TC (any precision): FP64-level accuracy with the
+                               projections, Gram-Schmidt Grams and updates, Ritz vectors and
+                               re-contraction on the tensor cores (qpgpu_gram_tc / qpgpu_lincomb_tc),
+                               the small Cholesky-QR Gram and update, step and residual norms in
+                               FP64, the Ritz vectors of FP32-sigma iterations in FP32 (they only
+                               feed the step) */
   int32_t dressed;          /* 1: davidson_diag_mrcc_hs2 (plugins/MRCC_Utils/davidson.irp.f:496-553):
                                sigma and H_jj carry the context's dressing (qpgpu_set_dressing) */
   int32_t reserved;         /* 0 */
