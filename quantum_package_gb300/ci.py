@@ -7,9 +7,10 @@ reference, on top of the device library.
   ``read_wf`` is set and the file's ``mo_label`` matches.
 * ``ci_electronic_energy`` is ``CI_electronic_energy`` / ``CI_eigenvectors`` /
   ``CI_eigenvectors_s2`` (src/Davidson/diagonalize_CI.irp.f:22-165).  The
-  guess is ``psi_coef`` for the first min(N_states, N_det) vectors and zero
-  up to N_states_diag.  The "Davidson" branch is davidson_diag_HS2 on the
-  device.  The "Lapack" branch diagonalises the dense H assembled from the
+  guess is ``psi_coef`` for the first min(N_states, N_det) vectors; the
+  "Davidson" branch (davidson_diag_HS2 on the device) fills the others with
+  seeded normal vectors, as davidson_diag_hjj_sjj draws them
+  (diagonalization_hs2.irp.f:188-200).  The "Lapack" branch diagonalises the dense H assembled from the
   device's pair elements and diagonal, and picks states by S^2 as the
   reference does when s2_eig is set.
 * ``ci_energy`` adds the nuclear repulsion (:1-20).  ``diagonalize_ci``
@@ -88,10 +89,25 @@ def dense_h(wf):
     return H
 
 
-def ci_electronic_energy(wf, psi_coef, n_states, n_states_diag=None, algorithm="Davidson", s2_eig=True,
-                         expected_s2=None, threshold=1e-12, davidson_sze_max=8, **davidson_kw):
-    """CI_electronic_energy, CI_eigenvectors (N_det, N_states_diag) and CI_eigenvectors_s2."""
+N_DET_MAX_JACOBI = 2000  # src/Determinants/EZFIO.cfg default
+
+
+def diag_algorithm(n_det, n_states, n_det_max_jacobi=N_DET_MAX_JACOBI):
+    """The diag_algorithm provider (src/Determinants/determinants.irp.f:3-17):
+    Davidson above N_det_max_jacobi determinants, else Lapack, and Lapack
+    when N_det < N_states."""
+    alg = "Davidson" if n_det > n_det_max_jacobi else "Lapack"
+    return "Lapack" if n_det < n_states else alg
+
+
+def ci_electronic_energy(wf, psi_coef, n_states, n_states_diag=None, algorithm=None, s2_eig=True,
+                         expected_s2=None, threshold=1e-12, davidson_sze_max=8, seed=0,
+                         n_det_max_jacobi=N_DET_MAX_JACOBI, **davidson_kw):
+    """CI_electronic_energy, CI_eigenvectors (N_det, N_states_diag) and
+    CI_eigenvectors_s2; ``algorithm`` None follows diag_algorithm."""
     n = wf.n_det
+    if algorithm is None:
+        algorithm = diag_algorithm(n, n_states, n_det_max_jacobi)
     nsd = n_states if n_states_diag is None else n_states_diag
     if expected_s2 is None:
         sz = 0.5 * (wf.n_alpha - wf.n_beta)
@@ -100,6 +116,11 @@ def ci_electronic_energy(wf, psi_coef, n_states, n_states_diag=None, algorithm="
     k = min(n_states, n)
     guess[:, :k] = np.asarray(psi_coef)[:, :k]
     if algorithm == "Davidson":
+        # davidson_diag_hjj_sjj draws the guesses beyond N_states from a
+        # normal distribution (diagonalization_hs2.irp.f:188-200); seeded here
+        rng = np.random.default_rng(seed)
+        for c in range(k, min(n, nsd)):
+            guess[:, c] = rng.normal(size=n)
         r = wf.davidson_diag_hs2(np.ascontiguousarray(guess[:, :min(n, nsd)].T), min(n, n_states),
                                  davidson_sze_max=davidson_sze_max, threshold=threshold, s2_eig=s2_eig,
                                  **davidson_kw)

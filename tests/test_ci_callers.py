@@ -24,6 +24,15 @@ from quantum_package_gb300 import ci, ezfio
 from quantum_package_gb300 import generate as G
 
 
+def test_diag_algorithm_rule():
+    # determinants.irp.f:3-17: Davidson above N_det_max_jacobi, Lapack below
+    # it and whenever N_det < N_states
+    assert ci.diag_algorithm(2001, 1) == "Davidson"
+    assert ci.diag_algorithm(2000, 1) == "Lapack"
+    assert ci.diag_algorithm(3, 4) == "Lapack"
+    assert ci.diag_algorithm(500, 2, n_det_max_jacobi=100) == "Davidson"
+
+
 def test_psi_coef_guess_reads_matching_label(tmp_path):
     n = 40
     g = ci.psi_coef_guess(n, 3)
@@ -82,7 +91,8 @@ def test_ci_energy_davidson_and_lapack_branches():
     w = np.linalg.eigvalsh(H)
     wf = Wavefunction.from_problem(p)
     guess = ci.psi_coef_guess(p.n_det, 2)
-    rd = ci.ci_electronic_energy(wf, guess, 2, n_states_diag=4, s2_eig=False, threshold=1e-12, max_iter=400)
+    rd = ci.ci_electronic_energy(wf, guess, 2, n_states_diag=4, algorithm="Davidson", s2_eig=False,
+                                 threshold=1e-12, max_iter=400)
     rl = ci.ci_electronic_energy(wf, guess, 2, n_states_diag=4, algorithm="Lapack", s2_eig=False)
     np.testing.assert_allclose(rd["energies"][:2], w[:2], rtol=0, atol=1e-9)
     np.testing.assert_allclose(rl["energies"], w[:4], rtol=0, atol=1e-9)
