@@ -61,7 +61,7 @@ constexpr int SBLK = 256;
 constexpr int SEL_TILE = 16384;    // FP64 numerators per CTA at most (128 KB of shared memory)
 constexpr int SEL_DTILE = 256;     // selectors staged per filtering pass
 constexpr int SEL_MAXST = 8;       // states
-constexpr int SEL_MAXFG = 2048;    // earlier generators kept per item (checked, not assumed)
+constexpr int SEL_MAXFG = 2048;    // earlier generators kept per item in shared memory (else read from the global list)
 
 enum { IT_SINGLE = 0, IT_SAME = 1, IT_AB = 2 };
 
@@ -323,10 +323,7 @@ __global__ void __launch_bounds__(SBLK) k_sel_items(SelArgs A) {
       for (int w = 0; w < 2 * NINT; ++w) k += popc64(mask[w] & ~q[w]);
       if (k <= 2) {
         const int slot = atomicAdd(&nfg, 1);
-        if (slot < SEL_MAXFG)
-          fgen[slot] = gp;
-        else
-          atomicOr(A.err, 1);
+        if (slot < SEL_MAXFG) fgen[slot] = gp;  // past SEL_MAXFG the bans read the global list
       }
     }
   }
@@ -435,8 +432,12 @@ __global__ void __launch_bounds__(SBLK) k_sel_items(SelArgs A) {
     set_orb(a, NINT, sp1, p1, true);
     if (it.kind != IT_SINGLE) set_orb(a, NINT, sp2, p2, true);
     bool banned = in_wf<NINT>(A, a);
-    for (int f = 0; f < min(nfg, SEL_MAXFG) && !banned; ++f)
-      banned = exc_deg<NINT>(a, A.dets + (int64_t)fgen[f] * 2 * NINT) <= 2;
+    if (nfg <= SEL_MAXFG) {
+      for (int f = 0; f < nfg && !banned; ++f) banned = exc_deg<NINT>(a, A.dets + (int64_t)fgen[f] * 2 * NINT) <= 2;
+    } else {  // more earlier generators reach this item than the shared list holds
+      for (int64_t f = A.flist_off[it.gl]; f < A.flist_off[it.gl + 1] && !banned; ++f)
+        banned = exc_deg<NINT>(a, A.dets + (int64_t)A.flist[f] * 2 * NINT) <= 2;
+    }
     if (banned) continue;
     ++next;
     // diag_H_mat_elem_fock (slater_rules.irp.f:1800-1866); holes and
@@ -695,9 +696,6 @@ static int run_selection(qpgpu_ctx* c, const double* coef, int n_st, const doubl
     if (buf_size == 0 || hcnt[1] <= cap) break;
     cap = hcnt[1];  // every candidate counted: run once more with room for all of them
   }
-  int herr = 0;
-  QP_CUDA(c, cudaMemcpy(&herr, d_err.p, sizeof(int), cudaMemcpyDeviceToHost));
-  if (herr) return qpgpu_fail(c, QPGPU_ERR_ARG, "select_pt2: more than 2048 earlier generators reach one work item");
   k_sel_pt2<<<1, 32, 0, st>>>((const double*)d_part.p, n_items, n_st, (double*)d_pt2.p);
   QP_CUDA(c, cudaMemcpyAsync(pt2, d_pt2.p, n_st * sizeof(double), cudaMemcpyDeviceToHost, st));
   if (per_gen) {

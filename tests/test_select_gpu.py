@@ -127,3 +127,33 @@ def test_select_end_to_end_and_refusals():
     with pytest.raises(QPGPUError):
         wf.select_pt2(np.ascontiguousarray(coefs.T), w[:2], 5, 4, 10)
     wf.close()
+
+
+@pytest.mark.gpu
+def test_select_many_generators_per_item():
+    # 10,000 generators: work items of late generators are reached by more
+    # earlier generators than the kernel's shared list holds (2,048), so the
+    # bans read the global list; the result must still equal the oracle's
+    from quantum_package_gb300.sigma import Wavefunction
+    n_mo, ne, nd = 10, 3, 10000
+    ints = G.make_integrals(n_mo, 29)
+    full = G.full_ci_dets(n_mo, ne, ne)
+    rng = np.random.default_rng(2)
+    dets = full[np.sort(rng.choice(len(full), nd, replace=False))]
+    c = rng.normal(size=(1, nd)) * np.exp(-np.arange(nd) / 5000.0)
+    # the overflow is reached: count, for the last generator's first alpha-beta
+    # hole pair, the earlier generators that lack at most 2 of its electrons
+    g = dets[-1]
+    occ_a = [o for o in range(n_mo) if (int(g[0, 0]) >> o) & 1]
+    occ_b = [o for o in range(n_mo) if (int(g[1, 0]) >> o) & 1]
+    mask = g.copy()
+    mask[0, 0] = np.uint64(int(mask[0, 0]) & ~(1 << occ_a[0]))
+    mask[1, 0] = np.uint64(int(mask[1, 0]) & ~(1 << occ_b[0]))
+    lack = [bin(int(mask[0, 0]) & ~int(d[0, 0])).count("1") + bin(int(mask[1, 0]) & ~int(d[1, 0])).count("1")
+            for d in dets[:-1]]
+    assert sum(1 for k in lack if k <= 2) > 2048
+    o = Oracle(n_mo, ne, ne, ints.h, ints.eri, dets)
+    wf = Wavefunction(n_mo, ne, ne, ints.h, ints.eri, dets)
+    e0 = np.array([-10.0])  # below every H_aa of this space: all denominators of one sign
+    _compare(wf.select_pt2(c, e0, nd, nd, 300), o.select_pt2(c, e0, nd, nd, 300))
+    wf.close()
