@@ -63,7 +63,7 @@ typedef struct qpgpu_info {
   int64_t device_bytes;   /* device memory held by the context */
   int64_t n_split_rows;   /* rows whose pairs span several sigma work chunks */
   int32_t direct_sigma;   /* 1: pairs not stored, sigma enumerates them at each call */
-  int32_t reserved;
+  int32_t n_keyed_lines;  /* beta columns + alpha rows with deletion-key tables */
 } qpgpu_info;
 
 /* Context for one orbital space; replaces the IRPF90 providers N_int,
@@ -90,6 +90,22 @@ int qpgpu_get_info(qpgpu_ctx* ctx, qpgpu_info* info);
 #define QPGPU_SIGMA_STORED 1
 #define QPGPU_SIGMA_DIRECT 2
 int qpgpu_set_sigma_mode(qpgpu_ctx* ctx, int mode);
+
+/* How the pair scans reach the partners of a determinant (no counterpart in
+ * the reference, whose loops test every string of the lines involved,
+ * u0Hu0.irp.f:177-332).  A beta column (alpha row) holding more than
+ * min_single determinants gets a table of its alpha (beta) strings with one
+ * electron removed, which the alpha x beta scan probes instead of scanning the
+ * line; one holding more than min_double gets a table with two electrons
+ * removed, which its own determinants probe for their same-spin pairs.  The
+ * pairs, and so sigma, are the same either way; only the work changes (a few
+ * heavy lines carry most of the scan work of large sets).  -1 keeps a default
+ * (min_single 64 (n_elec + 2), min_double 16384); INT64_MAX turns tables off.
+ * hash_bits (1..64, default 64) keeps the low bits of the key hashes only, to
+ * test that colliding keys still give the exact pairs.  Tables that would
+ * take more than half of the free device memory are left out.  Takes effect
+ * at the next qpgpu_set_dets. */
+int qpgpu_set_line_keys(qpgpu_ctx* ctx, int64_t min_single, int64_t min_double, int hash_bits);
 
 /* u_0_H_u_0 (src/Davidson/diagonalization_hs2.irp.f:446-484), the psi_energy
  * provider's routine: e_0[i] = <u_0(:,i)|H|u_0(:,i)> over the N_det rows of the

@@ -4,7 +4,7 @@ The compute path is libqpgpu.so (CUDA, sm_103a) behind the C-ABI of
 include/qpgpu.h; this package holds its Python mirror of the reference
 interface and the seeded input generator.
 """
-from ._lib import (ALGEBRA_FAST, ALGEBRA_FP64, ALGEBRA_TC, FF, FP32, FP64, SIGMA_AUTO, SIGMA_DIRECT,  # noqa: F401
-                   SIGMA_STORED, QPGPUError)
+from ._lib import (ALGEBRA_FAST, ALGEBRA_FP64, ALGEBRA_TC, FF, FP32, FP64, KEYS_OFF, SIGMA_AUTO,  # noqa: F401
+                   SIGMA_DIRECT, SIGMA_STORED, QPGPUError)
 
 __all__ = ["FP32", "FP64", "QPGPUError"]

@@ -18,6 +18,7 @@ ERRORS = {
 }
 FP64, FP32, FF = 0, 1, 2
 SIGMA_AUTO, SIGMA_STORED, SIGMA_DIRECT = 0, 1, 2  # qpgpu_set_sigma_mode
+KEYS_OFF = 2**63 - 1  # qpgpu_set_line_keys threshold: no deletion-key tables
 ALGEBRA_FAST, ALGEBRA_FP64, ALGEBRA_TC = 0, 1, 2  # qpgpu_davidson_params.algebra
 
 HEADER = os.path.join(os.path.dirname(os.path.dirname(os.path.abspath(__file__))), "include", "qpgpu.h")
@@ -33,7 +34,7 @@ class Info(C.Structure):
     _fields_ = [("n_det", C.c_int64), ("n_alpha_unique", C.c_int32), ("n_beta_unique", C.c_int32),
                 ("n_pairs", C.c_int64), ("n_s2_pairs", C.c_int64), ("setup_ms", C.c_double),
                 ("ref_energy", C.c_double), ("device_bytes", C.c_int64),
-                ("n_split_rows", C.c_int64), ("direct_sigma", C.c_int32), ("reserved", C.c_int32)]
+                ("n_split_rows", C.c_int64), ("direct_sigma", C.c_int32), ("n_keyed_lines", C.c_int32)]
 
 
 class DavidsonParams(C.Structure):
@@ -84,6 +85,7 @@ def load():
         "qpgpu_last_error": (C.c_char_p, [vp]),
         "qpgpu_get_info": (C.c_int, [vp, C.POINTER(Info)]),
         "qpgpu_set_sigma_mode": (C.c_int, [vp, C.c_int]),
+        "qpgpu_set_line_keys": (C.c_int, [vp, C.c_int64, C.c_int64, C.c_int]),
         "qpgpu_u0_h_u0": (C.c_int, [vp, vp, vp, C.c_int, C.c_int64]),
         "qpgpu_set_integrals": (C.c_int, [vp, vp, vp]),
         "qpgpu_set_dets": (C.c_int, [vp, vp, C.c_int64]),

@@ -285,11 +285,13 @@ int qpgpu_get_info(qpgpu_ctx* c, qpgpu_info* info) {
   if (c->have_dets) b += N * (32 * c->nint + 4 * 8) + 8 * (int64_t)(c->Ua + c->Ub) * c->nint;
   if (c->have_pairs && !c->direct) b += P * 16 + c->P_s2 * 8 + N * 28;
   if (c->have_pairs && c->direct) b += N * 24;
+  for (int k = 0; k < KT_N; ++k) b += c->kslots[k] * (int64_t)sizeof(KeySlot) + c->kmem_n[k] * 4;
+  if (c->have_dets) b += c->Ua + c->Ub;
   b += (int64_t)c->work_bytes;
   info->device_bytes = b;
   info->n_split_rows = c->items.n_multi;
   info->direct_sigma = c->direct ? 1 : 0;
-  info->reserved = 0;
+  info->n_keyed_lines = c->n_keyed_lines;
   return QPGPU_OK;
 }
 
@@ -299,6 +301,17 @@ int qpgpu_set_sigma_mode(qpgpu_ctx* c, int mode) {
     return qpgpu_fail(c, QPGPU_ERR_ARG, "sigma mode must be QPGPU_SIGMA_AUTO, _STORED or _DIRECT");
   Lock l(c->mu);
   c->sigma_mode = mode;
+  return QPGPU_OK;
+}
+
+int qpgpu_set_line_keys(qpgpu_ctx* c, int64_t min_single, int64_t min_double, int hash_bits) {
+  if (!c) return QPGPU_ERR_ARG;
+  if (min_single < -1 || min_double < -1 || hash_bits < 1 || hash_bits > 64)
+    return qpgpu_fail(c, QPGPU_ERR_ARG, "line keys: thresholds must be >= -1 and hash_bits in 1..64");
+  Lock l(c->mu);
+  c->key_min_single = min_single;
+  c->key_min_double = min_double;
+  c->key_hash_bits = hash_bits;
   return QPGPU_OK;
 }
 

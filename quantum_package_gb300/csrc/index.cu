@@ -208,11 +208,15 @@ __global__ void k_csr_ptr(const int* src, int* ptr, int64_t t, int U) {
   }
 }
 
-// cost of the alpha-beta scan strategies, summed over the singles of each string
-__global__ void k_single_costs(const int* ptr, const int* idx, const int* loc, int64_t* cost, int U) {
+// cost of the alpha-beta scan strategies, summed over the singles of each
+// string: the length of each single's line, or keycost for a line with a
+// 1-deletion table (probes of the ne keys, about one warp step each)
+__global__ void k_single_costs(const int* ptr, const int* idx, const int* loc, const unsigned char* lkey,
+                               int64_t keycost, int64_t* cost, int U) {
   for (int64_t u = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; u < U; u += (int64_t)gridDim.x * blockDim.x) {
     int64_t c = 0;
-    for (int t = ptr[u]; t < ptr[u + 1]; ++t) c += loc[idx[t] + 1] - loc[idx[t]];
+    for (int t = ptr[u]; t < ptr[u + 1]; ++t)
+      c += (lkey && (lkey[idx[t]] & KEY_SINGLE)) ? keycost : loc[idx[t] + 1] - loc[idx[t]];
     cost[u] = c;
   }
 }
@@ -349,6 +353,7 @@ int singles_adjacency(qpgpu_ctx* c, const u64* uniq, int U, int ne, int** ptr_ou
 }  // namespace
 
 void qp_free_dets(qpgpu_ctx* c) {
+  qp_free_line_keys(c);
   void** ps[] = {(void**)&c->d_dets, (void**)&c->d_alpha, (void**)&c->d_beta, (void**)&c->d_rows,
                  (void**)&c->d_cols, (void**)&c->d_order, (void**)&c->d_col_loc, (void**)&c->d_t_order,
                  (void**)&c->d_t_cols, (void**)&c->d_row_loc, (void**)&c->d_sa_ptr, (void**)&c->d_sa_idx,
@@ -437,10 +442,15 @@ int qp_build_index(qpgpu_ctx* c) {
   rc = singles_adjacency(c, c->d_beta, Ub, c->nb, &c->d_sb_ptr, &c->d_sb_idx, &c->n_sb);
   if (rc) return rc;
   qp_mark(c, "singles adjacency");
+  rc = qp_build_line_keys(c);
+  if (rc) return rc;
+  qp_mark(c, "deletion-key tables");
   QP_CUDA(c, dev_alloc(&c->d_cost_a, (size_t)Ua));
   QP_CUDA(c, dev_alloc(&c->d_cost_b, (size_t)Ub));
-  k_single_costs<<<grid_for(Ua), TPB, 0, st>>>(c->d_sa_ptr, c->d_sa_idx, c->d_row_loc, c->d_cost_a, Ua);
-  k_single_costs<<<grid_for(Ub), TPB, 0, st>>>(c->d_sb_ptr, c->d_sb_idx, c->d_col_loc, c->d_cost_b, Ub);
+  k_single_costs<<<grid_for(Ua), TPB, 0, st>>>(c->d_sa_ptr, c->d_sa_idx, c->d_row_loc, c->d_rowkey,
+                                               32 * (int64_t)(c->nb + 2), c->d_cost_a, Ua);
+  k_single_costs<<<grid_for(Ub), TPB, 0, st>>>(c->d_sb_ptr, c->d_sb_idx, c->d_col_loc, c->d_colkey,
+                                               32 * (int64_t)(c->na + 2), c->d_cost_b, Ub);
   QP_CUDA(c, cudaGetLastError());
   QP_CUDA(c, cudaStreamSynchronize(st));
   return 0;

@@ -23,6 +23,7 @@
 // singles of b (as the reference does) or the rows of the alpha singles of a,
 // whichever holds fewer determinants.
 #include <algorithm>
+#include <climits>
 #include <vector>
 
 #include <cub/cub.cuh>
@@ -94,6 +95,11 @@ struct BuildArgs {
   int64_t blk_off;
   int write_s2;
   int tag_t;
+  // deletion-key tables of the heavy lines (keys.cu); colkey / rowkey null: none
+  KeyView kv[KT_N];
+  const unsigned char* colkey;
+  const unsigned char* rowkey;
+  u64 hmask;
 };
 
 constexpr unsigned QP_TAG_T = 0x80000000u;  // column given as alpha-major position
@@ -127,14 +133,13 @@ __global__ void __launch_bounds__(BLK) k_class_a(BuildArgs a) {
   if (r0 >= a.N) return;
   const int64_t k = r0 + threadIdx.x;
   const bool valid = k < a.N;
-  const int64_t rl = min(r0 + BLK, a.N) - 1;
-  const int U0 = a.col_loc[a.cols[r0]];
-  const int U1 = a.col_loc[a.cols[rl] + 1];
   int cs = 0, ce = 0;
   u64 my[2 * NINT];
   int64_t out = 0;
+  bool keyed = false;  // the column has a 2-deletion table: k_same_keyed takes the row
   if (valid) {
     const int b = a.cols[k];
+    keyed = a.colkey && (a.colkey[b] & KEY_DOUBLE);
     cs = a.col_loc[b];
     ce = a.col_loc[b + 1];
     const int ai = a.rows[k];
@@ -146,7 +151,20 @@ __global__ void __launch_bounds__(BLK) k_class_a(BuildArgs a) {
     if (FILL) out = a.rowptr[k] - a.col_base;
   }
   int cnt = 0;
-  const bool act = valid && (MODE == MODE_COUNT || dsel(a, k));
+  const bool act = valid && !keyed && (MODE == MODE_COUNT || dsel(a, k));
+  // the tiles span the columns of the block's active rows
+  __shared__ int s_lo, s_hi;
+  if (threadIdx.x == 0) {
+    s_lo = INT_MAX;
+    s_hi = INT_MIN;
+  }
+  __syncthreads();
+  if (act) {
+    atomicMin(&s_lo, cs);
+    atomicMax(&s_hi, ce);
+  }
+  __syncthreads();
+  const int U0 = s_lo, U1 = s_hi;
   for (int t0 = U0; t0 < U1; t0 += TILE) {
     const int tn = min(TILE, U1 - t0);
     __syncthreads();
@@ -171,7 +189,7 @@ __global__ void __launch_bounds__(BLK) k_class_a(BuildArgs a) {
       }
     }
   }
-  if (MODE == MODE_COUNT && valid) a.cntA[k] = cnt;
+  if (MODE == MODE_COUNT && valid && !keyed) a.cntA[k] = cnt;
 }
 
 // ---- class B: same alpha row, beta singles / doubles ----------------------
@@ -183,15 +201,14 @@ __global__ void __launch_bounds__(BLK) k_class_b(BuildArgs a) {
   if (q0 >= a.N) return;
   const int64_t q = q0 + threadIdx.x;
   const bool valid = q < a.N;
-  const int64_t ql = min(q0 + BLK, a.N) - 1;
-  const int V0 = a.row_loc[a.rows[a.t_order[q0]]];
-  const int V1 = a.row_loc[a.rows[a.t_order[ql]] + 1];
   int rs = 0, re = 0;
   int64_t k = 0, out = 0;
   u64 my[2 * NINT];
+  bool keyed = false;  // the row has a 2-deletion table: k_same_keyed takes it
   if (valid) {
     k = a.t_order[q];
     const int ai = a.rows[k], bi = a.cols[k];
+    keyed = a.rowkey && (a.rowkey[ai] & KEY_DOUBLE);
     rs = a.row_loc[ai];
     re = a.row_loc[ai + 1];
 #pragma unroll
@@ -202,7 +219,19 @@ __global__ void __launch_bounds__(BLK) k_class_b(BuildArgs a) {
     if (FILL) out = a.rowptr[k] + a.cntA[k] - a.col_base;
   }
   int cnt = 0;
-  const bool act = valid && (MODE == MODE_COUNT || dsel(a, k));
+  const bool act = valid && !keyed && (MODE == MODE_COUNT || dsel(a, k));
+  __shared__ int s_lo, s_hi;
+  if (threadIdx.x == 0) {
+    s_lo = INT_MAX;
+    s_hi = INT_MIN;
+  }
+  __syncthreads();
+  if (act) {
+    atomicMin(&s_lo, rs);
+    atomicMax(&s_hi, re);
+  }
+  __syncthreads();
+  const int V0 = s_lo, V1 = s_hi;
   for (int t0 = V0; t0 < V1; t0 += TILE) {
     const int tn = min(TILE, V1 - t0);
     __syncthreads();
@@ -227,7 +256,7 @@ __global__ void __launch_bounds__(BLK) k_class_b(BuildArgs a) {
       }
     }
   }
-  if (MODE == MODE_COUNT && valid) a.cntB[k] = cnt;
+  if (MODE == MODE_COUNT && valid && !keyed) a.cntB[k] = cnt;
 }
 
 // spin flip test of an alpha-single x beta-single pair: the two excitations
@@ -245,9 +274,13 @@ __device__ __forceinline__ bool spin_flip(const u64* my, const u64* ca, const u6
 }
 
 // ---- class C: alpha single x beta single, one warp per row ----------------
+// A column (row) with a 1-deletion table is not scanned: the lanes probe the
+// row's alpha (beta) string with each electron removed, and the members of
+// each group are the alpha (beta) singles of the row in that column (row).
 template <int NINT, int MODE>
 __global__ void __launch_bounds__(BLK) k_class_c(BuildArgs a) {
   constexpr bool FILL = MODE == MODE_FILL;
+  constexpr unsigned FULL = 0xffffffffu;
   const int lane = threadIdx.x & 31;
   const int64_t warp = ((int64_t)blockIdx.x * BLK + threadIdx.x) >> 5;
   const int64_t nwarp = ((int64_t)gridDim.x * BLK) >> 5;
@@ -267,6 +300,39 @@ __global__ void __launch_bounds__(BLK) k_class_c(BuildArgs a) {
       sout = a.s2ptr[k];
     }
     int cnt = 0, scnt = 0;
+    // 32 candidates, one per lane: hit = (ca, cb) is an alpha single x beta
+    // single of the row; col is what the fill writes, jpos the bilinear position
+    auto step = [&](bool hit, const u64* ca, const u64* cb, int col, int jpos) {
+      const unsigned bal = __ballot_sync(FULL, hit);
+      const bool flip = hit && spin_flip<NINT>(my, ca, cb);
+      const unsigned sbal = __ballot_sync(FULL, flip);
+      if (FILL && hit) {  // elements: k_pair_values; S^2 values of spin flips here
+        const int64_t o = out + cnt + __popc(bal & lt);
+        if (o < a.rowptr[k + 1] - a.col_base)
+          a.colidx[o] = col;
+        else
+          atomicOr(a.err, 4);
+        if (flip && a.write_s2) {
+          u64 J[2 * NINT];
+#pragma unroll
+          for (int w = 0; w < NINT; ++w) {
+            J[w] = ca[w];
+            J[NINT + w] = cb[w];
+          }
+          double s2;
+          h_double_ab<NINT>(a.t, my, J, &s2, nullptr, nullptr);
+          const int64_t so = sout + scnt + __popc(sbal & lt);
+          if (so < a.s2ptr[k + 1]) {
+            a.s2col[so] = jpos;
+            a.s2val[so] = (float)s2;
+          } else {
+            atomicOr(a.err, 8);
+          }
+        }
+      }
+      cnt += __popc(bal);
+      scnt += __popc(sbal);
+    };
     const bool by_cols = a.cost_b[bi] <= a.cost_a[ai];
     if (by_cols) {
       for (int t = a.sb_ptr[bi]; t < a.sb_ptr[bi + 1]; ++t) {
@@ -274,8 +340,57 @@ __global__ void __launch_bounds__(BLK) k_class_c(BuildArgs a) {
         u64 cb[NINT];
 #pragma unroll
         for (int w = 0; w < NINT; ++w) cb[w] = a.beta[(int64_t)bp * NINT + w];
-        const int end = a.col_loc[bp + 1];
-        for (int p0 = a.col_loc[bp]; p0 < end; p0 += 32) {
+        const int beg = a.col_loc[bp], end = a.col_loc[bp + 1];
+        if (a.colkey && (a.colkey[bp] & KEY_SINGLE)) {
+          // keyed column: the lanes probe the row's alpha string minus each
+          // electron; the members of a group are its alpha singles there
+          const KeyView& kv = a.kv[KT_COL1];
+          for (int e0 = 0; e0 < a.t.na; e0 += 32) {
+            unsigned gs = 0, gl = 0;
+            u64 K[NINT];
+#pragma unroll
+            for (int w = 0; w < NINT; ++w) K[w] = my[w];
+            if (e0 + lane < a.t.na) {
+              const int eb = nth_electron<NINT>(my, e0 + lane);
+              clear_orbital<NINT>(K, eb);
+              if (!key_find(kv, key_hash<NINT>(KT_COL1, bp, K, a.hmask), gs, gl)) gl = 0;
+            }
+            const int nr = min(32, a.t.na - e0);
+            for (int r = 0; r < nr; ++r) {
+              const unsigned s0 = __shfl_sync(FULL, gs, r), n0 = __shfl_sync(FULL, gl, r);
+              if (n0 == 0) continue;
+              u64 Kr[NINT];
+#pragma unroll
+              for (int w = 0; w < NINT; ++w) Kr[w] = __shfl_sync(FULL, K[w], r);
+              for (unsigned t0 = 0; t0 < n0; t0 += 32) {
+                const unsigned tt = t0 + lane;
+                int pos = -1;
+                if (tt < n0) {
+                  pos = kv.mem[s0 + tt];
+                  if (tt > 0 && kv.mem[s0 + tt - 1] == pos) pos = -1;  // repeated member (colliding keys)
+                }
+                bool hit = false;
+                u64 ca[NINT];
+#pragma unroll
+                for (int w = 0; w < NINT; ++w) ca[w] = 0;
+                if (pos >= beg && pos < end) {
+                  int d = 0;
+                  bool eq = true;
+#pragma unroll
+                  for (int w = 0; w < NINT; ++w) {
+                    ca[w] = a.alpha_pos[(int64_t)pos * NINT + w];
+                    d += popc64(my[w] ^ ca[w]);
+                    eq &= (my[w] & ca[w]) == Kr[w];
+                  }
+                  hit = d == 2 && eq;
+                }
+                step(hit, ca, cb, pos, pos);
+              }
+            }
+          }
+          continue;
+        }
+        for (int p0 = beg; p0 < end; p0 += 32) {
           const int pos = p0 + lane;
           bool hit = false;
           u64 ca[NINT];
@@ -288,35 +403,7 @@ __global__ void __launch_bounds__(BLK) k_class_c(BuildArgs a) {
             }
             hit = (d == 2);
           }
-          const unsigned bal = __ballot_sync(0xffffffffu, hit);
-          const bool flip = hit && spin_flip<NINT>(my, ca, cb);
-          const unsigned sbal = __ballot_sync(0xffffffffu, flip);
-          if (FILL && hit) {  // elements: k_pair_values; S^2 values of spin flips here
-            const int64_t o = out + cnt + __popc(bal & lt);
-            if (o < a.rowptr[k + 1] - a.col_base)
-              a.colidx[o] = pos;
-            else
-              atomicOr(a.err, 4);
-            if (flip && a.write_s2) {
-              u64 J[2 * NINT];
-#pragma unroll
-              for (int w = 0; w < NINT; ++w) {
-                J[w] = ca[w];
-                J[NINT + w] = cb[w];
-              }
-              double s2;
-              h_double_ab<NINT>(a.t, my, J, &s2, nullptr, nullptr);
-              const int64_t so = sout + scnt + __popc(sbal & lt);
-              if (so < a.s2ptr[k + 1]) {
-                a.s2col[so] = pos;
-                a.s2val[so] = (float)s2;
-              } else {
-                atomicOr(a.err, 8);
-              }
-            }
-          }
-          cnt += __popc(bal);
-          scnt += __popc(sbal);
+          step(hit, ca, cb, pos, pos);
         }
       }
     } else {
@@ -325,11 +412,62 @@ __global__ void __launch_bounds__(BLK) k_class_c(BuildArgs a) {
         u64 ca[NINT];
 #pragma unroll
         for (int w = 0; w < NINT; ++w) ca[w] = a.alpha[(int64_t)ap * NINT + w];
-        const int end = a.row_loc[ap + 1];
-        for (int q0 = a.row_loc[ap]; q0 < end; q0 += 32) {
+        const int beg = a.row_loc[ap], end = a.row_loc[ap + 1];
+        if (a.rowkey && (a.rowkey[ap] & KEY_SINGLE)) {
+          // keyed row: the same with the row's beta string
+          const KeyView& kv = a.kv[KT_ROW1];
+          for (int e0 = 0; e0 < a.t.nb; e0 += 32) {
+            unsigned gs = 0, gl = 0;
+            u64 K[NINT];
+#pragma unroll
+            for (int w = 0; w < NINT; ++w) K[w] = my[NINT + w];
+            if (e0 + lane < a.t.nb) {
+              const int eb = nth_electron<NINT>(my + NINT, e0 + lane);
+              clear_orbital<NINT>(K, eb);
+              if (!key_find(kv, key_hash<NINT>(KT_ROW1, ap, K, a.hmask), gs, gl)) gl = 0;
+            }
+            const int nr = min(32, a.t.nb - e0);
+            for (int r = 0; r < nr; ++r) {
+              const unsigned s0 = __shfl_sync(FULL, gs, r), n0 = __shfl_sync(FULL, gl, r);
+              if (n0 == 0) continue;
+              u64 Kr[NINT];
+#pragma unroll
+              for (int w = 0; w < NINT; ++w) Kr[w] = __shfl_sync(FULL, K[w], r);
+              for (unsigned t0 = 0; t0 < n0; t0 += 32) {
+                const unsigned tt = t0 + lane;
+                int q = -1;
+                if (tt < n0) {
+                  q = kv.mem[s0 + tt];
+                  if (tt > 0 && kv.mem[s0 + tt - 1] == q) q = -1;
+                }
+                bool hit = false;
+                u64 cb[NINT];
+#pragma unroll
+                for (int w = 0; w < NINT; ++w) cb[w] = 0;
+                int jpos = 0;
+                if (q >= beg && q < end) {
+                  int d = 0;
+                  bool eq = true;
+#pragma unroll
+                  for (int w = 0; w < NINT; ++w) {
+                    cb[w] = a.beta_tpos[(int64_t)q * NINT + w];
+                    d += popc64(my[NINT + w] ^ cb[w]);
+                    eq &= (my[NINT + w] & cb[w]) == Kr[w];
+                  }
+                  hit = d == 2 && eq;
+                  if (hit) jpos = a.t_order[q];
+                }
+                step(hit, ca, cb, a.tag_t ? (int)(QP_TAG_T | (unsigned)q) : jpos, jpos);
+              }
+            }
+          }
+          continue;
+        }
+        for (int q0 = beg; q0 < end; q0 += 32) {
           const int q = q0 + lane;
           bool hit = false;
           u64 cb[NINT];
+          int jpos = 0;
           if (q < end) {
             int d = 0;
 #pragma unroll
@@ -338,37 +476,9 @@ __global__ void __launch_bounds__(BLK) k_class_c(BuildArgs a) {
               d += popc64(my[NINT + w] ^ cb[w]);
             }
             hit = (d == 2);
+            if (hit) jpos = a.t_order[q];
           }
-          const unsigned bal = __ballot_sync(0xffffffffu, hit);
-          const bool flip = hit && spin_flip<NINT>(my, ca, cb);
-          const unsigned sbal = __ballot_sync(0xffffffffu, flip);
-          if (FILL && hit) {  // elements: k_pair_values; S^2 values of spin flips here
-            const int64_t o = out + cnt + __popc(bal & lt);
-            const int jpos = a.t_order[q];
-            if (o < a.rowptr[k + 1] - a.col_base)
-              a.colidx[o] = a.tag_t ? (int)(QP_TAG_T | (unsigned)q) : jpos;
-            else
-              atomicOr(a.err, 4);
-            if (flip && a.write_s2) {
-              u64 J[2 * NINT];
-#pragma unroll
-              for (int w = 0; w < NINT; ++w) {
-                J[w] = ca[w];
-                J[NINT + w] = cb[w];
-              }
-              double s2;
-              h_double_ab<NINT>(a.t, my, J, &s2, nullptr, nullptr);
-              const int64_t so = sout + scnt + __popc(sbal & lt);
-              if (so < a.s2ptr[k + 1]) {
-                a.s2col[so] = jpos;
-                a.s2val[so] = (float)s2;
-              } else {
-                atomicOr(a.err, 8);
-              }
-            }
-          }
-          cnt += __popc(bal);
-          scnt += __popc(sbal);
+          step(hit, ca, cb, a.tag_t ? (int)(QP_TAG_T | (unsigned)q) : jpos, jpos);
         }
       }
     }
@@ -376,6 +486,117 @@ __global__ void __launch_bounds__(BLK) k_class_c(BuildArgs a) {
       a.cntC[k] = cnt;
       a.cntS[k] = scnt;
     }
+  }
+}
+
+// ---- same-spin pairs of the rows of keyed lines, one warp per row ----------
+// SPIN 0: rows of a beta column with a 2-deletion table (class A), SPIN 1:
+// rows of an alpha row with one (class B).  The lanes probe 32 of the row's
+// C(ne,2) keys at a time; then the warp walks each group, lanes over members.
+// A member y of the key K of x is a double when |x ^ y| = 4 and x & y = K,
+// and a single when |x ^ y| = 2 and K is x & y without its lowest electron:
+// each pair is accepted under exactly one key, whatever the hash collisions.
+template <int NINT, int MODE, int SPIN>
+__global__ void __launch_bounds__(BLK) k_same_keyed(BuildArgs a) {
+  constexpr bool FILL = MODE == MODE_FILL;
+  constexpr unsigned FULL = 0xffffffffu;
+  constexpr int kind = SPIN == 0 ? KT_COL2 : KT_ROW2;
+  const int lane = threadIdx.x & 31;
+  const int64_t warp = ((int64_t)blockIdx.x * BLK + threadIdx.x) >> 5;
+  const int64_t nwarp = ((int64_t)gridDim.x * BLK) >> 5;
+  const unsigned lt = (1u << lane) - 1u;
+  const KeyView kv = a.kv[kind];
+  const int ne = SPIN == 0 ? a.t.na : a.t.nb;
+  const int nc = ne * (ne - 1) / 2;
+  const unsigned char* lflag = SPIN == 0 ? a.colkey : a.rowkey;
+  const u64* strs = SPIN == 0 ? a.alpha_pos : a.beta_tpos;
+  const int64_t lo = MODE == MODE_COUNT ? 0 : a.row_lo, hi = MODE == MODE_COUNT ? a.N : a.row_hi;
+  if (lflag == nullptr) return;
+  for (int64_t k = lo + warp; k < hi; k += nwarp) {
+    const int line = SPIN == 0 ? a.cols[k] : a.rows[k];
+    if (!(lflag[line] & KEY_DOUBLE)) continue;
+    if (MODE != MODE_COUNT && !dsel(a, k)) continue;
+    u64 x[NINT];
+#pragma unroll
+    for (int w = 0; w < NINT; ++w)
+      x[w] = SPIN == 0 ? a.alpha_pos[k * NINT + w] : a.beta[(int64_t)a.cols[k] * NINT + w];
+    const int ls = SPIN == 0 ? a.col_loc[line] : a.row_loc[line];
+    const int le = SPIN == 0 ? a.col_loc[line + 1] : a.row_loc[line + 1];
+    int64_t out = 0;
+    int cap = 0;
+    if (FILL) {
+      out = a.rowptr[k] + (SPIN == 0 ? 0 : a.cntA[k]) - a.col_base;
+      cap = SPIN == 0 ? a.cntA[k] : a.cntB[k];
+    }
+    int cnt = 0;
+    for (int c0 = 0; c0 < nc; c0 += 32) {
+      unsigned gs = 0, gl = 0;
+      u64 K[NINT];
+#pragma unroll
+      for (int w = 0; w < NINT; ++w) K[w] = 0;
+      if (c0 + lane < nc) {
+        int i, j;
+        pair_of_combo(c0 + lane, ne, i, j);
+        const int bi = nth_electron<NINT>(x, i), bj = nth_electron<NINT>(x, j);
+#pragma unroll
+        for (int w = 0; w < NINT; ++w) K[w] = x[w];
+        clear_orbital<NINT>(K, bi);
+        clear_orbital<NINT>(K, bj);
+        if (!key_find(kv, key_hash<NINT>(kind, line, K, a.hmask), gs, gl)) gl = 0;
+      }
+      const int nr = min(32, nc - c0);
+      for (int r = 0; r < nr; ++r) {
+        const unsigned s0 = __shfl_sync(FULL, gs, r), n0 = __shfl_sync(FULL, gl, r);
+        if (n0 == 0) continue;
+        u64 Kr[NINT];
+#pragma unroll
+        for (int w = 0; w < NINT; ++w) Kr[w] = __shfl_sync(FULL, K[w], r);
+        for (unsigned t0 = 0; t0 < n0; t0 += 32) {
+          const unsigned t = t0 + lane;
+          bool hit = false;
+          int p = 0;
+          if (t < n0) {
+            p = kv.mem[s0 + t];
+            const bool dup = t > 0 && kv.mem[s0 + t - 1] == p;
+            if (!dup && p >= ls && p < le) {
+              u64 m[NINT];
+              int d = 0;
+#pragma unroll
+              for (int w = 0; w < NINT; ++w) {
+                const u64 y = strs[(int64_t)p * NINT + w];
+                d += popc64(x[w] ^ y);
+                m[w] = x[w] & y;
+              }
+              if (d == 2) {  // canonical key of a single: drop the lowest common electron
+                bool done = false;
+#pragma unroll
+                for (int w = 0; w < NINT; ++w)
+                  if (!done && m[w]) {
+                    m[w] &= m[w] - 1;
+                    done = true;
+                  }
+              }
+              if (d == 2 || d == 4) {
+                bool eq = true;
+#pragma unroll
+                for (int w = 0; w < NINT; ++w) eq &= m[w] == Kr[w];
+                hit = eq;
+              }
+            }
+          }
+          const unsigned bal = __ballot_sync(FULL, hit);
+          if (FILL && hit) {
+            const int o = cnt + __popc(bal & lt);
+            if (o < cap)
+              a.colidx[out + o] = SPIN == 0 ? p : (a.tag_t ? (int)(QP_TAG_T | (unsigned)p) : a.t_order[p]);
+            else
+              atomicOr(a.err, SPIN == 0 ? 1 : 2);
+          }
+          cnt += __popc(bal);
+        }
+      }
+    }
+    if (MODE == MODE_COUNT && lane == 0) (SPIN == 0 ? a.cntA : a.cntB)[k] = cnt;
   }
 }
 
@@ -488,6 +709,14 @@ BuildArgs index_args(const qpgpu_ctx* c) {
   a.blk_off = 0;
   a.write_s2 = 1;
   a.tag_t = 0;
+  for (int t = 0; t < KT_N; ++t) {
+    a.kv[t].slot = c->d_kslot[t];
+    a.kv[t].mask = c->kslots[t] > 0 ? (u64)(c->kslots[t] - 1) : 0ull;
+    a.kv[t].mem = c->d_kmem[t];
+  }
+  a.colkey = c->d_colkey;
+  a.rowkey = c->d_rowkey;
+  a.hmask = c->key_hash_bits >= 64 ? ~0ull : ((1ull << std::max(1, c->key_hash_bits)) - 1ull);
   return a;
 }
 
@@ -509,8 +738,10 @@ int build_pairs_t(qpgpu_ctx* c) {
   const unsigned gC = nblocks(N * 32, BLK);
   qp_mark(c, "pair setup");
   k_class_a<NINT, MODE_COUNT><<<gAB, BLK, 0, st>>>(a);
+  k_same_keyed<NINT, MODE_COUNT, 0><<<gC, BLK, 0, st>>>(a);
   qp_mark(c, "count A (same beta)");
   k_class_b<NINT, MODE_COUNT><<<gAB, BLK, 0, st>>>(a);
+  k_same_keyed<NINT, MODE_COUNT, 1><<<gC, BLK, 0, st>>>(a);
   qp_mark(c, "count B (same alpha)");
   k_class_c<NINT, MODE_COUNT><<<gC, BLK, 0, st>>>(a);
   qp_mark(c, "count C (alpha x beta)");
@@ -582,8 +813,10 @@ int build_pairs_t(qpgpu_ctx* c) {
   a.err = err.p;
   qp_mark(c, "scan + alloc");
   k_class_a<NINT, MODE_FILL><<<gAB, BLK, 0, st>>>(a);
+  k_same_keyed<NINT, MODE_FILL, 0><<<gC, BLK, 0, st>>>(a);
   qp_mark(c, "fill A");
   k_class_b<NINT, MODE_FILL><<<gAB, BLK, 0, st>>>(a);
+  k_same_keyed<NINT, MODE_FILL, 1><<<gC, BLK, 0, st>>>(a);
   qp_mark(c, "fill B");
   k_class_c<NINT, MODE_FILL><<<gC, BLK, 0, st>>>(a);
   qp_mark(c, "fill C");
@@ -728,8 +961,11 @@ int sigma_direct_t(qpgpu_ctx* c, double* v, double* s, const double* u, const do
       a.col_base = rp[lo];
       a.blk_off = lo / BLK;
       const unsigned gA = (unsigned)((hi - 1) / BLK - lo / BLK + 1);
+      const unsigned gK = nblocks((hi - lo) * 32, BLK);
       k_class_a<NINT, MODE_FILL><<<gA, BLK, 0, st>>>(a);
+      k_same_keyed<NINT, MODE_FILL, 0><<<gK, BLK, 0, st>>>(a);
       k_class_b<NINT, MODE_FILL><<<gAB, BLK, 0, st>>>(a);
+      k_same_keyed<NINT, MODE_FILL, 1><<<gK, BLK, 0, st>>>(a);
       k_class_c<NINT, MODE_FILL><<<gC, BLK, 0, st>>>(a);
       k_pair_sigma<NINT><<<nblocks((hi - lo) * 32, BLK), BLK, 0, st>>>(a, c->d_direct_cols);
     }

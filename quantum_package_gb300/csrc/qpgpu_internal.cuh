@@ -284,6 +284,100 @@ __device__ __forceinline__ double diag_s(const u64* det) {
 #endif  // __CUDACC__
 
 // ---------------------------------------------------------------------------
+// Deletion-key tables of heavy lines (built by keys.cu, read by the pair scans)
+//
+// Two spin strings one excitation apart share exactly one string with one
+// electron removed (their intersection); two strings two excitations apart
+// share exactly one string with two electrons removed.  For a line (a beta
+// column or an alpha row) that holds many determinants, the pair scans look
+// the line's strings up by these deletion keys instead of testing every
+// string of the line: a table maps hash(kind, line, key) to the group of
+// positions whose strings produced the key.  Every group member is verified
+// exactly (position inside the line, popcount of the difference, the key
+// itself), so hash collisions only add candidates, never pairs.
+// ---------------------------------------------------------------------------
+struct __align__(16) KeySlot {
+  u64 h;           // hash of (kind, line, key); 0 = empty slot
+  unsigned start;  // first member of the group in the table's member array
+  unsigned len;    // members in the group
+};
+struct KeyView {
+  const KeySlot* slot;  // open addressing, linear probing; nullptr = no table
+  u64 mask;             // slots - 1 (a power of two)
+  const int* mem;       // positions (bilinear for columns, alpha-major for rows), grouped
+};
+// tables: 1-deletion keys of the alpha strings of heavy columns / of the beta
+// strings of heavy rows (alpha x beta pairs), 2-deletion keys (same-spin pairs)
+enum { KT_COL1 = 0, KT_ROW1 = 1, KT_COL2 = 2, KT_ROW2 = 3, KT_N = 4 };
+// per-line flags: the line has a 1-deletion / a 2-deletion table
+constexpr unsigned char KEY_SINGLE = 1, KEY_DOUBLE = 2;
+
+#ifdef __CUDACC__
+// SplitMix64 output function (Steele, Lea and Flood, "Fast splittable
+// pseudorandom number generators", OOPSLA 2014) as the mixing step
+__device__ __forceinline__ u64 key_mix(u64 z) {
+  z = (z ^ (z >> 30)) * 0xbf58476d1ce4e5b9ull;
+  z = (z ^ (z >> 27)) * 0x94d049bb133111ebull;
+  return z ^ (z >> 31);
+}
+// never 0 (the empty slot); hmask keeps the low bits only (a test hook that
+// makes distinct keys collide)
+template <int NINT>
+__device__ __forceinline__ u64 key_hash(int kind, int line, const u64* K, u64 hmask) {
+  u64 h = key_mix((((u64)(unsigned)line) << 2 | (u64)kind) + 0x9e3779b97f4a7c15ull);
+#pragma unroll
+  for (int w = 0; w < NINT; ++w) h = key_mix(h ^ K[w]);
+  return (h & hmask) | 1ull;
+}
+__device__ __forceinline__ bool key_find(const KeyView& kv, u64 h, unsigned& start, unsigned& len) {
+  if (kv.slot == nullptr) return false;
+  u64 s = h & kv.mask;
+  for (u64 it = 0; it <= kv.mask; ++it) {
+    const KeySlot sl = kv.slot[s];
+    if (sl.h == h) {
+      start = sl.start;
+      len = sl.len;
+      return true;
+    }
+    if (sl.h == 0) return false;
+    s = (s + 1) & kv.mask;
+  }
+  return false;
+}
+// orbital index (word * 64 + bit) of the j-th electron (0-based) of s
+template <int NINT>
+__device__ __forceinline__ int nth_electron(const u64* s, int j) {
+#pragma unroll
+  for (int w = 0; w < NINT; ++w) {
+    const int c = __popcll(s[w]);
+    if (j < c) {
+      u64 v = s[w];
+      for (int t = 0; t < j; ++t) v &= v - 1;
+      return w * 64 + __ffsll((long long)v) - 1;
+    }
+    j -= c;
+  }
+  return -1;
+}
+// clear orbital b (word * 64 + bit) of s, with constant word indices (s stays in registers)
+template <int NINT>
+__device__ __forceinline__ void clear_orbital(u64* s, int b) {
+#pragma unroll
+  for (int w = 0; w < NINT; ++w)
+    if (w == (b >> 6)) s[w] &= ~(1ull << (b & 63));
+}
+// pair (i, j), i < j, of the c-th 2-electron combination of ne electrons
+__device__ __forceinline__ void pair_of_combo(int c, int ne, int& i, int& j) {
+  i = 0;
+  while (c >= ne - 1 - i) {
+    c -= ne - 1 - i;
+    ++i;
+  }
+  j = i + 1 + c;
+}
+#endif  // __CUDACC__
+
+// ---------------------------------------------------------------------------
 // Host-side context
 // ---------------------------------------------------------------------------
 struct DevBuf {
@@ -405,6 +499,18 @@ struct qpgpu_ctx {
   // per-row strategy cost of the alpha-beta class
   int64_t* d_cost_b = nullptr;  // per unique beta: sum of |col(b')| over singles b'
   int64_t* d_cost_a = nullptr;  // per unique alpha: sum of |row(a')| over singles a'
+  // deletion-key tables of heavy lines (keys.cu)
+  KeySlot* d_kslot[KT_N] = {nullptr, nullptr, nullptr, nullptr};
+  int64_t kslots[KT_N] = {0, 0, 0, 0};
+  int* d_kmem[KT_N] = {nullptr, nullptr, nullptr, nullptr};
+  int64_t kmem_n[KT_N] = {0, 0, 0, 0};
+  unsigned char* d_colkey = nullptr;  // per beta column: KEY_SINGLE | KEY_DOUBLE
+  unsigned char* d_rowkey = nullptr;  // per alpha row
+  int n_keyed_lines = 0;
+  // qpgpu_set_line_keys: lines holding more determinants than these get
+  // tables (-1: defaults), and the hash bits kept
+  int64_t key_min_single = -1, key_min_double = -1;
+  int key_hash_bits = 64;
 
   // Hamiltonian in CSR over bilinear rows (columns are bilinear positions)
   bool have_pairs = false;
@@ -471,6 +577,8 @@ inline void dev_free(void* p) {
 
 // entry points implemented across translation units
 int qp_build_index(qpgpu_ctx* c);      // index.cu
+int qp_build_line_keys(qpgpu_ctx* c);  // keys.cu (inside qp_build_index)
+void qp_free_line_keys(qpgpu_ctx* c);  // keys.cu
 int qp_build_pairs(qpgpu_ctx* c);      // pairs.cu
 void qp_free_dets(qpgpu_ctx* c);       // index.cu
 void qp_free_pairs(qpgpu_ctx* c);      // pairs.cu

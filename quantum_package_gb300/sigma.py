@@ -37,7 +37,8 @@ def stream_handle(stream):
 class Wavefunction:
     """Providers of one orbital space and determinant set, on the GPU."""
 
-    def __init__(self, n_mo: int, n_alpha: int, n_beta: int, h=None, eri=None, psi_det=None, sigma_mode=0):
+    def __init__(self, n_mo: int, n_alpha: int, n_beta: int, h=None, eri=None, psi_det=None, sigma_mode=0,
+                 line_keys=None):
         L = _lib.load()
         self.n_mo, self.n_alpha, self.n_beta = n_mo, n_alpha, n_beta
         self.n_int = (n_mo - 1) // 64 + 1
@@ -49,18 +50,28 @@ class Wavefunction:
         self.n_det = 0
         if sigma_mode:
             self.set_sigma_mode(sigma_mode)
+        if line_keys is not None:
+            self.set_line_keys(*line_keys)
         if h is not None:
             self.set_integrals(h, eri)
         if psi_det is not None:
             self.set_dets(psi_det)
 
     @classmethod
-    def from_problem(cls, prob, sigma_mode=0):
-        return cls(prob.n_mo, prob.n_alpha, prob.n_beta, prob.ints.h, prob.ints.eri, prob.dets, sigma_mode)
+    def from_problem(cls, prob, sigma_mode=0, line_keys=None):
+        return cls(prob.n_mo, prob.n_alpha, prob.n_beta, prob.ints.h, prob.ints.eri, prob.dets, sigma_mode,
+                   line_keys)
 
     def set_sigma_mode(self, mode):
         """SIGMA_AUTO (0), SIGMA_STORED (1) or SIGMA_DIRECT (2); takes effect at the next set_dets."""
         check(_lib.load().qpgpu_set_sigma_mode(self._ctx, int(mode)), self._ctx)
+
+    def set_line_keys(self, min_single=-1, min_double=-1, hash_bits=64):
+        """Deletion-key tables for the lines holding more than min_single /
+        min_double determinants (-1: defaults, KEYS_OFF: none); hash_bits < 64
+        only to test colliding keys.  Takes effect at the next set_dets."""
+        check(_lib.load().qpgpu_set_line_keys(self._ctx, int(min_single), int(min_double), int(hash_bits)),
+              self._ctx)
 
     def close(self):
         if getattr(self, "_ctx", None):
