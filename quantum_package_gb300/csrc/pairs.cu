@@ -278,7 +278,7 @@ __device__ __forceinline__ bool spin_flip(const u64* my, const u64* ca, const u6
 // row's alpha (beta) string with each electron removed, and the members of
 // each group are the alpha (beta) singles of the row in that column (row).
 template <int NINT, int MODE>
-__global__ void __launch_bounds__(BLK) k_class_c(BuildArgs a) {
+__global__ void __launch_bounds__(BLK, 2) k_class_c(BuildArgs a) {
   constexpr bool FILL = MODE == MODE_FILL;
   constexpr unsigned FULL = 0xffffffffu;
   const int lane = threadIdx.x & 31;
@@ -333,152 +333,170 @@ __global__ void __launch_bounds__(BLK) k_class_c(BuildArgs a) {
       cnt += __popc(bal);
       scnt += __popc(sbal);
     };
+    // Lines of the row's singles, 32 at a time: the lanes read the bounds of
+    // 32 lines at once, and the candidates of the scanned ones are packed
+    // into full warp steps (lane prefix sums over the line lengths), since
+    // most lines hold a few determinants; lines with a 1-deletion table are
+    // probed afterwards, one after the other.
     const bool by_cols = a.cost_b[bi] <= a.cost_a[ai];
-    if (by_cols) {
-      for (int t = a.sb_ptr[bi]; t < a.sb_ptr[bi + 1]; ++t) {
-        const int bp = a.sb_idx[t];
-        u64 cb[NINT];
+    const int t_beg = by_cols ? a.sb_ptr[bi] : a.sa_ptr[ai];
+    const int t_end = by_cols ? a.sb_ptr[bi + 1] : a.sa_ptr[ai + 1];
+    const int* lidx = by_cols ? a.sb_idx : a.sa_idx;
+    const int* lloc = by_cols ? a.col_loc : a.row_loc;
+    const unsigned char* lkey = by_cols ? a.colkey : a.rowkey;
+    for (int t0 = t_beg; t0 < t_end; t0 += 32) {
+      const int t = t0 + lane;
+      int ln = -1, beg = 0, len = 0;
+      bool kl = false;
+      if (t < t_end) {
+        ln = lidx[t];
+        beg = lloc[ln];
+        kl = lkey && (lkey[ln] & KEY_SINGLE);
+        if (!kl) len = lloc[ln + 1] - beg;
+      }
+      int incl = len;
 #pragma unroll
-        for (int w = 0; w < NINT; ++w) cb[w] = a.beta[(int64_t)bp * NINT + w];
-        const int beg = a.col_loc[bp], end = a.col_loc[bp + 1];
-        if (a.colkey && (a.colkey[bp] & KEY_SINGLE)) {
-          // keyed column: the lanes probe the row's alpha string minus each
-          // electron; the members of a group are its alpha singles there
-          const KeyView& kv = a.kv[KT_COL1];
-          for (int e0 = 0; e0 < a.t.na; e0 += 32) {
-            unsigned gs = 0, gl = 0;
-            u64 K[NINT];
+      for (int o = 1; o < 32; o <<= 1) {
+        const int y = __shfl_up_sync(FULL, incl, o);
+        if (lane >= o) incl += y;
+      }
+      const int total = __shfl_sync(FULL, incl, 31);
+      for (int c0 = 0; c0 < total; c0 += 32) {
+        const int ci = c0 + lane;
+        int src = 0;  // first lane whose inclusive prefix exceeds ci
 #pragma unroll
-            for (int w = 0; w < NINT; ++w) K[w] = my[w];
-            if (e0 + lane < a.t.na) {
-              const int eb = nth_electron<NINT>(my, e0 + lane);
-              clear_orbital<NINT>(K, eb);
-              if (!key_find(kv, key_hash<NINT>(KT_COL1, bp, K, a.hmask), gs, gl)) gl = 0;
-            }
-            const int nr = min(32, a.t.na - e0);
-            for (int r = 0; r < nr; ++r) {
-              const unsigned s0 = __shfl_sync(FULL, gs, r), n0 = __shfl_sync(FULL, gl, r);
-              if (n0 == 0) continue;
-              u64 Kr[NINT];
-#pragma unroll
-              for (int w = 0; w < NINT; ++w) Kr[w] = __shfl_sync(FULL, K[w], r);
-              for (unsigned t0 = 0; t0 < n0; t0 += 32) {
-                const unsigned tt = t0 + lane;
-                int pos = -1;
-                if (tt < n0) {
-                  pos = kv.mem[s0 + tt];
-                  if (tt > 0 && kv.mem[s0 + tt - 1] == pos) pos = -1;  // repeated member (colliding keys)
-                }
-                bool hit = false;
-                u64 ca[NINT];
-#pragma unroll
-                for (int w = 0; w < NINT; ++w) ca[w] = 0;
-                if (pos >= beg && pos < end) {
-                  int d = 0;
-                  bool eq = true;
-#pragma unroll
-                  for (int w = 0; w < NINT; ++w) {
-                    ca[w] = a.alpha_pos[(int64_t)pos * NINT + w];
-                    d += popc64(my[w] ^ ca[w]);
-                    eq &= (my[w] & ca[w]) == Kr[w];
-                  }
-                  hit = d == 2 && eq;
-                }
-                step(hit, ca, cb, pos, pos);
-              }
-            }
-          }
-          continue;
+        for (int st = 16; st > 0; st >>= 1) {
+          const int pr = __shfl_sync(FULL, incl, src + st - 1);
+          if (pr <= ci) src += st;
         }
-        for (int p0 = beg; p0 < end; p0 += 32) {
-          const int pos = p0 + lane;
-          bool hit = false;
-          u64 ca[NINT];
-          if (pos < end) {
-            int d = 0;
+        const int sbeg = __shfl_sync(FULL, beg, src), slen = __shfl_sync(FULL, len, src);
+        const int sinc = __shfl_sync(FULL, incl, src), sln = __shfl_sync(FULL, ln, src);
+        bool hit = false;
+        u64 ca[NINT], cb[NINT];
+#pragma unroll
+        for (int w = 0; w < NINT; ++w) ca[w] = cb[w] = 0;
+        int col = 0, jpos = 0;
+        if (ci < total) {
+          const int pos = sbeg + (ci - (sinc - slen));
+          int d = 0;
+          if (by_cols) {  // column sln (a beta single): alpha singles of the row
 #pragma unroll
             for (int w = 0; w < NINT; ++w) {
               ca[w] = a.alpha_pos[(int64_t)pos * NINT + w];
               d += popc64(my[w] ^ ca[w]);
             }
-            hit = (d == 2);
-          }
-          step(hit, ca, cb, pos, pos);
-        }
-      }
-    } else {
-      for (int t = a.sa_ptr[ai]; t < a.sa_ptr[ai + 1]; ++t) {
-        const int ap = a.sa_idx[t];
-        u64 ca[NINT];
+            hit = d == 2;
+            if (hit) {
 #pragma unroll
-        for (int w = 0; w < NINT; ++w) ca[w] = a.alpha[(int64_t)ap * NINT + w];
-        const int beg = a.row_loc[ap], end = a.row_loc[ap + 1];
-        if (a.rowkey && (a.rowkey[ap] & KEY_SINGLE)) {
-          // keyed row: the same with the row's beta string
-          const KeyView& kv = a.kv[KT_ROW1];
-          for (int e0 = 0; e0 < a.t.nb; e0 += 32) {
-            unsigned gs = 0, gl = 0;
-            u64 K[NINT];
-#pragma unroll
-            for (int w = 0; w < NINT; ++w) K[w] = my[NINT + w];
-            if (e0 + lane < a.t.nb) {
-              const int eb = nth_electron<NINT>(my + NINT, e0 + lane);
-              clear_orbital<NINT>(K, eb);
-              if (!key_find(kv, key_hash<NINT>(KT_ROW1, ap, K, a.hmask), gs, gl)) gl = 0;
+              for (int w = 0; w < NINT; ++w) cb[w] = a.beta[(int64_t)sln * NINT + w];
+              col = jpos = pos;
             }
-            const int nr = min(32, a.t.nb - e0);
-            for (int r = 0; r < nr; ++r) {
-              const unsigned s0 = __shfl_sync(FULL, gs, r), n0 = __shfl_sync(FULL, gl, r);
-              if (n0 == 0) continue;
-              u64 Kr[NINT];
-#pragma unroll
-              for (int w = 0; w < NINT; ++w) Kr[w] = __shfl_sync(FULL, K[w], r);
-              for (unsigned t0 = 0; t0 < n0; t0 += 32) {
-                const unsigned tt = t0 + lane;
-                int q = -1;
-                if (tt < n0) {
-                  q = kv.mem[s0 + tt];
-                  if (tt > 0 && kv.mem[s0 + tt - 1] == q) q = -1;
-                }
-                bool hit = false;
-                u64 cb[NINT];
-#pragma unroll
-                for (int w = 0; w < NINT; ++w) cb[w] = 0;
-                int jpos = 0;
-                if (q >= beg && q < end) {
-                  int d = 0;
-                  bool eq = true;
-#pragma unroll
-                  for (int w = 0; w < NINT; ++w) {
-                    cb[w] = a.beta_tpos[(int64_t)q * NINT + w];
-                    d += popc64(my[NINT + w] ^ cb[w]);
-                    eq &= (my[NINT + w] & cb[w]) == Kr[w];
-                  }
-                  hit = d == 2 && eq;
-                  if (hit) jpos = a.t_order[q];
-                }
-                step(hit, ca, cb, a.tag_t ? (int)(QP_TAG_T | (unsigned)q) : jpos, jpos);
-              }
-            }
-          }
-          continue;
-        }
-        for (int q0 = beg; q0 < end; q0 += 32) {
-          const int q = q0 + lane;
-          bool hit = false;
-          u64 cb[NINT];
-          int jpos = 0;
-          if (q < end) {
-            int d = 0;
+          } else {  // row sln (an alpha single): beta singles of the row
 #pragma unroll
             for (int w = 0; w < NINT; ++w) {
-              cb[w] = a.beta_tpos[(int64_t)q * NINT + w];
+              cb[w] = a.beta_tpos[(int64_t)pos * NINT + w];
               d += popc64(my[NINT + w] ^ cb[w]);
             }
-            hit = (d == 2);
-            if (hit) jpos = a.t_order[q];
+            hit = d == 2;
+            if (hit) {
+#pragma unroll
+              for (int w = 0; w < NINT; ++w) ca[w] = a.alpha[(int64_t)sln * NINT + w];
+              jpos = a.t_order[pos];
+              col = a.tag_t ? (int)(QP_TAG_T | (unsigned)pos) : jpos;
+            }
           }
-          step(hit, ca, cb, a.tag_t ? (int)(QP_TAG_T | (unsigned)q) : jpos, jpos);
+        }
+        step(hit, ca, cb, col, jpos);
+      }
+      unsigned kb = __ballot_sync(FULL, kl);
+      while (kb) {
+        const int L = __ffs(kb) - 1;
+        kb &= kb - 1;
+        const int kln = __shfl_sync(FULL, ln, L);
+        const int kbeg = lloc[kln], kend = lloc[kln + 1];
+        // keyed line: the lanes probe the row's string (alpha in a column,
+        // beta in a row) minus each electron; the members of a group are its
+        // singles in that line
+        u64 xs[NINT];  // the row's string of the probed spin
+#pragma unroll
+        for (int w = 0; w < NINT; ++w) xs[w] = by_cols ? my[w] : my[NINT + w];
+        const int ne = by_cols ? a.t.na : a.t.nb;
+        const int kind = by_cols ? KT_COL1 : KT_ROW1;
+        const KeyView& kv = a.kv[kind];
+        u64 fixed[NINT];  // the string of the line's other spin
+#pragma unroll
+        for (int w = 0; w < NINT; ++w) fixed[w] = by_cols ? a.beta[(int64_t)kln * NINT + w] : a.alpha[(int64_t)kln * NINT + w];
+        for (int e0 = 0; e0 < ne; e0 += 32) {
+          unsigned gs = 0, gl = 0;
+          u64 K[NINT];
+#pragma unroll
+          for (int w = 0; w < NINT; ++w) K[w] = xs[w];
+          if (e0 + lane < ne) {
+            const int eb = nth_electron<NINT>(K, e0 + lane);
+            clear_orbital<NINT>(K, eb);
+            if (!key_find(kv, key_hash<NINT>(kind, kln, K, a.hmask), gs, gl)) gl = 0;
+          }
+          // the members of the 32 probed groups, packed into full warp steps
+          int inc = (int)gl;
+#pragma unroll
+          for (int o = 1; o < 32; o <<= 1) {
+            const int y = __shfl_up_sync(FULL, inc, o);
+            if (lane >= o) inc += y;
+          }
+          const int tot = __shfl_sync(FULL, inc, 31);
+          for (int m0 = 0; m0 < tot; m0 += 32) {
+            const int mi = m0 + lane;
+            int src = 0;
+#pragma unroll
+            for (int st = 16; st > 0; st >>= 1) {
+              const int pr = __shfl_sync(FULL, inc, src + st - 1);
+              if (pr <= mi) src += st;
+            }
+            const unsigned s0 = __shfl_sync(FULL, gs, src);
+            const int i0 = __shfl_sync(FULL, inc, src) - (int)__shfl_sync(FULL, gl, src);
+            u64 Kr[NINT];
+#pragma unroll
+            for (int w = 0; w < NINT; ++w) Kr[w] = __shfl_sync(FULL, K[w], src);
+            {
+              int pos = -1;
+              if (mi < tot) {
+                const unsigned tt = (unsigned)(mi - i0);
+                pos = kv.mem[s0 + tt];
+                if (tt > 0 && kv.mem[s0 + tt - 1] == pos) pos = -1;  // repeated member (colliding keys)
+              }
+              bool hit = false;
+              u64 ca[NINT], cb[NINT];
+#pragma unroll
+              for (int w = 0; w < NINT; ++w) ca[w] = cb[w] = 0;
+              int col = 0, jpos = 0;
+              if (pos >= kbeg && pos < kend) {
+                int d = 0;
+                bool eq = true;
+                u64 y[NINT];
+#pragma unroll
+                for (int w = 0; w < NINT; ++w) {
+                  y[w] = by_cols ? a.alpha_pos[(int64_t)pos * NINT + w] : a.beta_tpos[(int64_t)pos * NINT + w];
+                  d += popc64(xs[w] ^ y[w]);
+                  eq &= (xs[w] & y[w]) == Kr[w];
+                }
+                hit = d == 2 && eq;
+                if (hit) {
+#pragma unroll
+                  for (int w = 0; w < NINT; ++w) {
+                    ca[w] = by_cols ? y[w] : fixed[w];
+                    cb[w] = by_cols ? fixed[w] : y[w];
+                  }
+                  if (by_cols) {
+                    col = jpos = pos;
+                  } else {
+                    jpos = a.t_order[pos];
+                    col = a.tag_t ? (int)(QP_TAG_T | (unsigned)pos) : jpos;
+                  }
+                }
+              }
+              step(hit, ca, cb, col, jpos);
+            }
+          }
         }
       }
     }
@@ -492,7 +510,8 @@ __global__ void __launch_bounds__(BLK) k_class_c(BuildArgs a) {
 // ---- same-spin pairs of the rows of keyed lines, one warp per row ----------
 // SPIN 0: rows of a beta column with a 2-deletion table (class A), SPIN 1:
 // rows of an alpha row with one (class B).  The lanes probe 32 of the row's
-// C(ne,2) keys at a time; then the warp walks each group, lanes over members.
+// C(ne,2) keys at a time; then the members of the 32 groups are packed into
+// full warp steps (most groups hold a few strings).
 // A member y of the key K of x is a double when |x ^ y| = 4 and x & y = K,
 // and a single when |x ^ y| = 2 and K is x & y without its lowest electron:
 // each pair is accepted under exactly one key, whatever the hash collisions.
@@ -544,18 +563,32 @@ __global__ void __launch_bounds__(BLK) k_same_keyed(BuildArgs a) {
         clear_orbital<NINT>(K, bj);
         if (!key_find(kv, key_hash<NINT>(kind, line, K, a.hmask), gs, gl)) gl = 0;
       }
-      const int nr = min(32, nc - c0);
-      for (int r = 0; r < nr; ++r) {
-        const unsigned s0 = __shfl_sync(FULL, gs, r), n0 = __shfl_sync(FULL, gl, r);
-        if (n0 == 0) continue;
+      // the members of the 32 probed groups, packed into full warp steps
+      int inc = (int)gl;
+#pragma unroll
+      for (int o = 1; o < 32; o <<= 1) {
+        const int y = __shfl_up_sync(FULL, inc, o);
+        if (lane >= o) inc += y;
+      }
+      const int tot = __shfl_sync(FULL, inc, 31);
+      for (int m0 = 0; m0 < tot; m0 += 32) {
+        const int mi = m0 + lane;
+        int src = 0;
+#pragma unroll
+        for (int st = 16; st > 0; st >>= 1) {
+          const int pr = __shfl_sync(FULL, inc, src + st - 1);
+          if (pr <= mi) src += st;
+        }
+        const unsigned s0 = __shfl_sync(FULL, gs, src);
+        const int i0 = __shfl_sync(FULL, inc, src) - (int)__shfl_sync(FULL, gl, src);
         u64 Kr[NINT];
 #pragma unroll
-        for (int w = 0; w < NINT; ++w) Kr[w] = __shfl_sync(FULL, K[w], r);
-        for (unsigned t0 = 0; t0 < n0; t0 += 32) {
-          const unsigned t = t0 + lane;
+        for (int w = 0; w < NINT; ++w) Kr[w] = __shfl_sync(FULL, K[w], src);
+        {
+          const unsigned t = (unsigned)(mi - i0);
           bool hit = false;
           int p = 0;
-          if (t < n0) {
+          if (mi < tot) {
             p = kv.mem[s0 + t];
             const bool dup = t > 0 && kv.mem[s0 + t - 1] == p;
             if (!dup && p >= ls && p < le) {
@@ -962,12 +995,18 @@ int sigma_direct_t(qpgpu_ctx* c, double* v, double* s, const double* u, const do
       a.blk_off = lo / BLK;
       const unsigned gA = (unsigned)((hi - 1) / BLK - lo / BLK + 1);
       const unsigned gK = nblocks((hi - lo) * 32, BLK);
+      const bool marks = st == c->stream;  // QPGPU_PROFILE=1: phase times on the context stream
+      if (marks) qp_mark(c, "direct: chunk start");
       k_class_a<NINT, MODE_FILL><<<gA, BLK, 0, st>>>(a);
       k_same_keyed<NINT, MODE_FILL, 0><<<gK, BLK, 0, st>>>(a);
+      if (marks) qp_mark(c, "direct: scan A");
       k_class_b<NINT, MODE_FILL><<<gAB, BLK, 0, st>>>(a);
       k_same_keyed<NINT, MODE_FILL, 1><<<gK, BLK, 0, st>>>(a);
+      if (marks) qp_mark(c, "direct: scan B");
       k_class_c<NINT, MODE_FILL><<<gC, BLK, 0, st>>>(a);
+      if (marks) qp_mark(c, "direct: scan C");
       k_pair_sigma<NINT><<<nblocks((hi - lo) * 32, BLK), BLK, 0, st>>>(a, c->d_direct_cols);
+      if (marks) qp_mark(c, "direct: elements");
     }
     clo = chi;
   }
@@ -1012,6 +1051,7 @@ int qp_sigma_direct(qpgpu_ctx* c, double* v, double* s, const double* u, int nst
                      : sigma_direct_t<2>(c, v, s, u, c->d_direct_ut, nst, st, row_lo, row_hi, row_first, row_step);
   if (rc) return rc;
   QP_CUDA(c, cudaGetLastError());
+  qp_report_marks(c);
   return 0;
 }
 

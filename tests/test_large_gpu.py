@@ -1,16 +1,17 @@
 """The 2e7-determinant configuration (16 alpha + 16 beta electrons in 120 MOs,
 N_int = 2, 2 states) on one GPU, end to end.  Opt-in (QPGPU_LARGE=1): the
-seeded set takes about 4 minutes to generate on the host, the set-up about a
-minute and each sigma about 70 s, since its 6.4e10 connected pairs do not fit
-in device memory and every sigma enumerates them (direct sigma).
+seeded set takes about 4 minutes to generate on the host; the set-up with its
+deletion-key tables about 2 s and each sigma about 6 s, since its 6.4e10
+connected pairs do not fit in device memory and every sigma enumerates them
+(direct sigma).
 
-Checks: the direct mode is chosen by itself; sigma and S^2 sigma are
-Hermitian (u0.Hu1 = u1.Hu0 to 1e-12 relative); 21 rows spread over the set
-match the CPU oracle's rows to 1e-12 relative; and five iterations of the
-device Davidson lower both Ritz values monotonically and bring the lowest
-state's squared residual norm (the reference's measure,
-diagonalization_hs2.irp.f:395) below 1e-3 from 4e5.  Run with -s to see the
-timings it prints.
+Checks: the direct mode is chosen by itself and the heavy lines get
+deletion-key tables; sigma and S^2 sigma are Hermitian (u0.Hu1 = u1.Hu0 to
+1e-12 relative); 21 rows spread over the set match the CPU oracle's rows to
+1e-12 relative; and the device Davidson (FP64, 8 vectors) lowers the ground
+state's Ritz value monotonically and brings its squared residual norm (the
+reference's measure, diagonalization_hs2.irp.f:395) below 1e-10 within 15
+iterations.  Run with -s to see the timings it prints.
 """
 import json
 import os
@@ -70,16 +71,20 @@ def test_large_direct_sigma_hermitian_and_oracle_rows(large):
 
 def test_large_davidson_iterations(large):
     prob, wf = large
+    assert wf.info()["n_keyed_lines"] > 0
     rng = np.random.default_rng(prob.seed)
-    u = rng.normal(size=(4, prob.n_det))
+    u = rng.normal(size=(8, prob.n_det))
     u[0] = 0.0
     u[0, 0] = 1.0
     t = time.time()
-    r = wf.davidson_diag_hs2(u, n_states=2, threshold=1e-10, s2_eig=False, max_iter=5)
+    r = wf.davidson_diag_hs2(u, n_states=2, threshold=1e-10, s2_eig=False, max_iter=15)
     tr = r["trace"]
     e, res = tr["energies"], tr["residuals"]
-    print(json.dumps({"wall_s": time.time() - t, "n_sigma": r["n_sigma"], "energies": e.tolist(),
-                      "residuals": res.tolist(), "elapsed_ms": tr["elapsed_ms"].tolist()}), flush=True)
-    assert r["n_sigma"] == 5 and len(e) == 5
-    assert np.all(np.diff(e, axis=0) <= 1e-9)  # Ritz values decrease (no restart within 5 iterations)
-    assert res[0, 0] > 1e3 and res[-1, 0] < 1e-3
+    first = np.nonzero(res[:, 0] < 1e-10)[0]
+    print(json.dumps({"wall_s": time.time() - t, "n_sigma": r["n_sigma"], "energies": e[-1, :2].tolist(),
+                      "residuals": res[-1, :2].tolist(),
+                      "ground_state_below_1e-10_at": int(first[0]) + 1 if len(first) else None,
+                      "elapsed_ms": tr["elapsed_ms"].tolist()}), flush=True)
+    assert r["n_sigma"] == 15
+    assert np.all(np.diff(e[:, 0]) <= 1e-9)  # the ground state's Ritz value never rises
+    assert res[0, 0] > 1e3 and res[-1, 0] < 1e-10
