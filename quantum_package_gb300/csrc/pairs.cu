@@ -6,8 +6,9 @@
 //   class A  J in the same beta column, alpha strings 1 or 2 apart  (:277-332)
 //   class B  J in the same alpha row, beta strings 1 or 2 apart      (:336-415)
 //   class C  alpha single x beta single                              (:177-246)
-// with the diagonal kept apart (:418-441).  Row k's segment of the CSR holds
-// its A hits (column order), then B hits (row order), then C hits.
+// with the diagonal kept apart (:418-441).  The fill writes row k's A hits,
+// then its B hits, then its C hits; the stored form then sorts each row's
+// columns ascending (the direct sigma keeps the fill order).
 //
 // Two passes run the same deterministic traversal: the first counts hits per
 // row, the second writes them (column = bilinear position of J, FP64 and FP32
@@ -753,6 +754,56 @@ BuildArgs index_args(const qpgpu_ctx* c) {
   return a;
 }
 
+__global__ void k_rel_offsets(const int64_t* rowptr, int64_t base, int* out, int64_t n) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+    out[i] = (int)(rowptr[i] - base);
+}
+
+// Each row's columns in ascending order (stored pairs, before the elements
+// are evaluated): neighbouring lanes of the sigma gathers then read
+// neighbouring coefficients, whatever order the scans and the deletion-key
+// probes found the partners in.  Segmented sorts over batches of rows of at
+// most 2^30 pairs.
+int sort_row_columns(qpgpu_ctx* c) {
+  const int64_t N = c->N, P = c->P;
+  cudaStream_t st = c->stream;
+  if (P == 0) return 0;
+  std::vector<int64_t> rp(N + 1);
+  QP_CUDA(c, cudaMemcpyAsync(rp.data(), c->d_rowptr, (N + 1) * sizeof(int64_t), cudaMemcpyDeviceToHost, st));
+  QP_CUDA(c, cudaStreamSynchronize(st));
+  const int64_t cap = std::min<int64_t>(P, (int64_t)1 << 30);
+  Scoped<int> tmp, offs;
+  Scoped<char> work;
+  size_t work_bytes = 0;
+  QP_CUDA(c, dev_alloc(&tmp.p, (size_t)cap));
+  QP_CUDA(c, dev_alloc(&offs.p, (size_t)N + 1));
+  for (int64_t r0 = 0; r0 < N;) {
+    int64_t r1 = std::upper_bound(rp.begin() + r0 + 1, rp.end(), rp[r0] + cap) - rp.begin() - 1;
+    if (r1 <= r0) r1 = r0 + 1;
+    const int64_t base = rp[r0], n = rp[r1] - base;
+    if (n > cap) return qpgpu_fail(c, QPGPU_ERR_NOMEM, "a row holds more than 2^30 pairs");
+    if (n > 0) {
+      k_rel_offsets<<<nblocks(r1 - r0 + 1, 256), 256, 0, st>>>(c->d_rowptr + r0, base, offs.p, r1 - r0 + 1);
+      size_t tb = 0;
+      QP_CUDA(c, cub::DeviceSegmentedSort::SortKeys(nullptr, tb, c->d_colidx + base, tmp.p, (int)n, (int)(r1 - r0),
+                                                    offs.p, offs.p + 1, st));
+      if (tb > work_bytes) {
+        dev_free(work.p);
+        work.p = nullptr;
+        QP_CUDA(c, dev_alloc(&work.p, tb));
+        work_bytes = tb;
+      }
+      QP_CUDA(c, cub::DeviceSegmentedSort::SortKeys(work.p, tb, c->d_colidx + base, tmp.p, (int)n, (int)(r1 - r0),
+                                                    offs.p, offs.p + 1, st));
+      QP_CUDA(c, cudaMemcpyAsync(c->d_colidx + base, tmp.p, (size_t)n * sizeof(int), cudaMemcpyDeviceToDevice, st));
+    }
+    r0 = r1;
+  }
+  QP_CUDA(c, cudaGetLastError());
+  QP_CUDA(c, cudaStreamSynchronize(st));
+  return 0;
+}
+
 template <int NINT>
 int build_pairs_t(qpgpu_ctx* c) {
   const int64_t N = c->N;
@@ -853,6 +904,16 @@ int build_pairs_t(qpgpu_ctx* c) {
   qp_mark(c, "fill B");
   k_class_c<NINT, MODE_FILL><<<gC, BLK, 0, st>>>(a);
   qp_mark(c, "fill C");
+  {
+    int herr = 0;
+    QP_CUDA(c, cudaMemcpyAsync(&herr, err.p, sizeof(int), cudaMemcpyDeviceToHost, st));
+    QP_CUDA(c, cudaStreamSynchronize(st));
+    if (herr)
+      return qpgpu_fail(c, QPGPU_ERR_STATE, "pair fill disagrees with pair count (" + std::to_string(herr) + ")");
+    const int rc = sort_row_columns(c);
+    if (rc) return rc;
+  }
+  qp_mark(c, "row columns sorted");
   k_pair_values<NINT><<<gC, BLK, 0, st>>>(a);
   qp_mark(c, "pair elements");
   QP_CUDA(c, cudaGetLastError());
