@@ -279,7 +279,7 @@ __device__ __forceinline__ bool spin_flip(const u64* my, const u64* ca, const u6
 // row's alpha (beta) string with each electron removed, and the members of
 // each group are the alpha (beta) singles of the row in that column (row).
 template <int NINT, int MODE>
-__global__ void __launch_bounds__(BLK, 2) k_class_c(BuildArgs a) {
+__global__ void __launch_bounds__(BLK, 3) k_class_c(BuildArgs a) {
   constexpr bool FILL = MODE == MODE_FILL;
   constexpr unsigned FULL = 0xffffffffu;
   const int lane = threadIdx.x & 31;
