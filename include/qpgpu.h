@@ -102,7 +102,9 @@ int qpgpu_set_sigma_mode(qpgpu_ctx* ctx, int mode);
  * heavy lines carry most of the scan work of large sets).  -1 keeps a default
  * (min_single 64 (n_elec + 2), min_double 16384); INT64_MAX turns tables off.
  * hash_bits (1..64, default 64) keeps the low bits of the key hashes only, to
- * test that colliding keys still give the exact pairs.  Tables that would
+ * test that colliding keys still give the exact pairs; below 64,
+ * qpgpu_set_dets refuses (QPGPU_ERR_ARG) a table of more than 2^22 keys,
+ * whose merged groups would make the scans quadratic.  Tables that would
  * take more than half of the free device memory are left out.  Takes effect
  * at the next qpgpu_set_dets. */
 int qpgpu_set_line_keys(qpgpu_ctx* ctx, int64_t min_single, int64_t min_double, int hash_bits);

@@ -167,6 +167,10 @@ int build_table(qpgpu_ctx* c, int kind, unsigned char* lflags, int nlines, int64
     QP_CUDA(c, cudaGetLastError());
     return 0;
   }
+  // cut hashes merge most keys into a few groups and make the probes walk
+  // them whole: a test hook for small sets only
+  if (c->key_hash_bits < 64 && E > ((int64_t)1 << 22))
+    return qpgpu_fail(c, QPGPU_ERR_ARG, "line keys: hash_bits below 64 is a test hook for tables of at most 2^22 keys");
   // the sort holds two copies of (hash, position): leave the lines to the
   // scans when that would take more than half of the free memory or the
   // member offsets would not fit 32 bits
