@@ -945,7 +945,7 @@ __global__ void k_alpha_major(const double* u, const int* t_order, double* uT, i
 // read from the alpha-major copy uT, where a row's partners are contiguous),
 // and the lanes are combined in a fixed butterfly order.
 template <int NINT>
-__global__ void __launch_bounds__(BLK) k_pair_sigma(BuildArgs a, const int* __restrict__ pc) {
+__global__ void __launch_bounds__(BLK, 3) k_pair_sigma(BuildArgs a, const int* __restrict__ pc) {
   const int lane = threadIdx.x & 31;
   const int64_t warp = ((int64_t)blockIdx.x * BLK + threadIdx.x) >> 5;
   const int64_t nwarp = ((int64_t)gridDim.x * BLK) >> 5;
@@ -959,24 +959,45 @@ __global__ void __launch_bounds__(BLK) k_pair_sigma(BuildArgs a, const int* __re
       my[NINT + w] = a.beta[(int64_t)bi * NINT + w];
     }
     double acc[8] = {0, 0, 0, 0, 0, 0, 0, 0}, sacc[8] = {0, 0, 0, 0, 0, 0, 0, 0};
-    const int64_t e1 = a.rowptr[k + 1];
-    for (int64_t e = a.rowptr[k] + lane; e < e1; e += 32) {
+    const int64_t e0 = a.rowptr[k], e1 = a.rowptr[k + 1];
+    // the fill wrote the row's same-beta partners, then its same-alpha
+    // partners, then the alpha x beta ones: a same-spin partner shares one
+    // string with the row, so only its other string is read
+    const int64_t eA = e0 + a.cntA[k], eB = eA + a.cntB[k];
+    for (int64_t e = e0 + lane; e < e1; e += 32) {
       const unsigned cj = (unsigned)pc[e - a.col_base];
       const bool via_t = (cj & QP_TAG_T) != 0;
       const int q = (int)(cj & ~QP_TAG_T);
-      const int j = via_t ? a.t_order[q] : q;
       u64 J[2 * NINT];
-      const int bj = a.cols[j];
-      bool samea = true, sameb = true;
-      int da = 0, db = 0;
+      bool samea, sameb;
+      int da = 0, db = 0, j = q;
+      if (e < eA) {  // same beta column: q is the partner's bilinear position
+        samea = false;
+        sameb = true;
 #pragma unroll
-      for (int w = 0; w < NINT; ++w) {
-        J[w] = a.alpha_pos[(int64_t)j * NINT + w];
-        J[NINT + w] = a.beta[(int64_t)bj * NINT + w];
-        samea &= J[w] == my[w];
-        sameb &= J[NINT + w] == my[NINT + w];
-        da += popc64(my[w] ^ J[w]);
-        db += popc64(my[NINT + w] ^ J[NINT + w]);
+        for (int w = 0; w < NINT; ++w) {
+          J[w] = a.alpha_pos[(int64_t)q * NINT + w];
+          J[NINT + w] = my[NINT + w];
+          da += popc64(my[w] ^ J[w]);
+        }
+      } else if (e < eB) {  // same alpha row: q is the partner's alpha-major position
+        samea = true;
+        sameb = false;
+#pragma unroll
+        for (int w = 0; w < NINT; ++w) {
+          J[w] = my[w];
+          J[NINT + w] = a.beta_tpos[(int64_t)q * NINT + w];
+          db += popc64(my[NINT + w] ^ J[NINT + w]);
+        }
+      } else {
+        j = via_t ? a.t_order[q] : q;
+        const int bj = a.cols[j];
+        samea = sameb = false;
+#pragma unroll
+        for (int w = 0; w < NINT; ++w) {
+          J[w] = a.alpha_pos[(int64_t)j * NINT + w];
+          J[NINT + w] = a.beta[(int64_t)bj * NINT + w];
+        }
       }
       double v, s2 = 0.0;
       if (sameb)
